@@ -1,0 +1,123 @@
+// nb_internal.cuh -- shared internals of libnbody_cuda.so (context, errors, scratch, math).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "nbody.h"
+
+// Bits of the device error word a kernel raises instead of trapping or spinning forever.
+enum : uint32_t {
+    NB_DEVERR_POOL = 1u << 0,
+    NB_DEVERR_DEPTH = 1u << 1,
+    NB_DEVERR_STACK = 1u << 2,
+    NB_DEVERR_TIMEOUT = 1u << 3,
+};
+
+struct nb_scratch_buf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+enum nb_scratch_slot : int {
+    NB_SCRATCH_NAIVE_F32 = 0,   // float4 sources for the FP32 pair kernel
+    NB_SCRATCH_ENERGY = 1,      // per-block partial energies
+    NB_SCRATCH_AABB = 2,        // per-block partial min/max
+    NB_SCRATCH_COUNT = 8,
+};
+
+struct nb_ctx {
+    int device = 0;
+    int sm_count = 0;
+    uint32_t* dev_error = nullptr;  // device error word (NB_DEVERR_* bits)
+    unsigned int* dev_counter = nullptr;  // last-block-done counters for fused grid reductions
+    nb_scratch_buf scratch[NB_SCRATCH_COUNT];
+};
+
+namespace nb {
+
+nb_status set_error(nb_status st, const char* fmt, ...);
+nb_status cuda_error(cudaError_t err, const char* what);
+// Grows scratch slot `slot` of the context to at least `bytes` (cudaMalloc; synchronous).
+nb_status scratch(nb_ctx* ctx, int slot, size_t bytes, void** out);
+nb_status check_launch(const char* what);
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace nb
+
+#define NB_CHECK_CTX(ctx)                                                                  \
+    do {                                                                                   \
+        if (!(ctx)) return nb::set_error(NB_ERR_INVALID_ARG, "%s: null context", __func__); \
+    } while (0)
+
+#define NB_TRY(expr)                     \
+    do {                                 \
+        nb_status _st = (expr);          \
+        if (_st != NB_OK) return _st;    \
+    } while (0)
+
+#define NB_CUDA_TRY(call)                                         \
+    do {                                                          \
+        cudaError_t _e = (call);                                  \
+        if (_e != cudaSuccess) return nb::cuda_error(_e, #call);  \
+    } while (0)
+
+// ---------------------------------------------------------------------------------------------
+// Device math.
+// ---------------------------------------------------------------------------------------------
+
+// FP64 reciprocal square root: hardware approximation of the high word refined by one
+// third-order Householder step (the Taylor series of (1-e)^(-1/2) = 1 + e/2 + 3e^2/8 + ...
+// with e = 1 - x*y0^2), which cubes the approximation's relative error (~2^-22 -> ~2^-66),
+// leaving only the final rounding (about 1 ulp).
+__device__ __forceinline__ double nb_rsqrt_f64(double x) {
+    double y0;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y0) : "d"(x));
+    const double t = x * y0;
+    const double e = fma(-t, y0, 1.0);
+    const double p = fma(0.375, e, 0.5);
+    const double u = y0 * e;
+    return fma(u, p, y0);
+}
+
+// FP32 reciprocal square root (MUFU.RSQ, ~2 ulp).
+__device__ __forceinline__ float nb_rsqrt_f32(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Packed FP32x2 arithmetic (sm_100+ f32x2 instructions): one instruction, two lanes.
+typedef unsigned long long nb_f2;
+__device__ __forceinline__ nb_f2 f2_pack(float lo, float hi) {
+    nb_f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(nb_f2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ nb_f2 f2_add(nb_f2 a, nb_f2 b) {
+    nb_f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ nb_f2 f2_sub(nb_f2 a, nb_f2 b) {
+    nb_f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ nb_f2 f2_mul(nb_f2 a, nb_f2 b) {
+    nb_f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ nb_f2 f2_fma(nb_f2 a, nb_f2 b, nb_f2 c) {
+    nb_f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
