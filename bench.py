@@ -1,0 +1,445 @@
+"""Benchmark of the Barnes-Hut step (and the naive pair kernels) on GB300.
+
+Default workload (the headline configuration): plain Barnes-Hut in FP64, theta = 0.5, the
+reference's per-body opening rule, N = 1,048,576 bodies of the seeded heliocentric disc, dt = 1 h.
+One step = leapfrog part 1 + octree build (AABB, keys, sort, cells, centre of mass) + traversal +
+leapfrog part 2, i.e. one iteration of BarnesHutAlgorithm::startSimulation's loop.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line on rank 0. `value` is device-resident throughput (steps/s summed over
+ranks); `e2e` times the same step through the C ABI with the state in pinned host memory,
+copied in and out every step. Multi-GPU: independent replicas (one per rank, no collective on
+the data path), `scaling: weak`. `--impl reference` times the CPU restatement of the reference
+(OpenMP, all host cores) on the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "n-body-simulation_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+N_BODIES = 1 << 20
+THETA = 0.5
+DT = 1.0 / 24
+EPS2 = 1e-22
+SEED = 1
+# kernels of ours launched per step: kick_drift 1, build 50 (aabb 1, keys 1, radix 8 x (hist 1 +
+# scan 3 + scatter 1), runs 1, splits 1, count 1, scan 3, emit 1, centre of mass 1),
+# traversal 1, kick 1
+LAUNCHES_PER_STEP = 53
+# algorithmic FLOP of the traversal (Nyland's 20 per pair interaction for an accepted cell; an
+# opened cell costs its distance test: 3 sub, 3 mul, 2 add, 1 rsqrt, 1 mul = 10)
+FLOP_ACCEPTED, FLOP_OPENED = 20, 10
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-i", str(self.device), "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [c.strip() for c in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_traffic(name):
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(name)
+    except (OSError, ValueError):
+        return None
+
+
+def measured_hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU baseline (the oracle: C++/OpenMP restatement of the reference, timed on the host cores)
+# ---------------------------------------------------------------------------------------------
+def cpu_bh_step_seconds(d, sample_fraction: float):
+    """One BH step of the restated reference on all host cores: leapfrog, full tree build and the
+    traversal of an evenly strided sample of the bodies (scaled to all bodies)."""
+    import numpy as np
+
+    import oracle
+    n = len(d["m"])
+    x, y, z = d["x"].copy(), d["y"].copy(), d["z"].copy()
+    v = [d["vx"].copy(), d["vy"].copy(), d["vz"].copy()]
+    a = [np.zeros(n), np.zeros(n), np.zeros(n)]
+    stride = max(1, int(round(1.0 / sample_fraction)))
+    targets = np.arange(0, n, stride, dtype=np.uint32)
+    t0 = time.perf_counter()
+    vh = oracle.leapfrog_part1(v, [x, y, z], a, DT)
+    t1 = time.perf_counter()
+    tree = oracle.build_subtrees(d["m"], x, y, z)
+    t2 = time.perf_counter()
+    oracle.bh_accel_subset(tree, x, y, z, targets, d["G"], EPS2, THETA)
+    t3 = time.perf_counter()
+    oracle.leapfrog_part2(v, vh, a, DT)
+    t4 = time.perf_counter()
+    trav = (t3 - t2) * (n / len(targets))
+    return (t1 - t0) + (t2 - t1) + trav + (t4 - t3), {"build_s": t2 - t1, "traversal_s": trav,
+                                                       "traversal_sample_bodies": len(targets)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from nbody import generators
+
+    d = generators.heliocentric_disc(N_BODIES, SEED)
+    cores = os.cpu_count()
+    # size the per-step traversal sample so that warmup + steps stay within ~2.5 minutes
+    probe_t, parts = cpu_bh_step_seconds(d, 1.0 / 64)
+    fixed = probe_t - parts["traversal_s"]
+    total_steps = args.steps + args.warmup
+    frac = 1.0
+    while frac > 1.0 / 64 and total_steps * (fixed + parts["traversal_s"] * frac) > 150:
+        frac /= 2
+    for _ in range(args.warmup):
+        cpu_bh_step_seconds(d, frac)
+    times = []
+    for _ in range(args.steps):
+        t, parts = cpu_bh_step_seconds(d, frac)
+        times.append(t)
+    t_step = sum(times) / len(times)
+    value = 1.0 / t_step
+    sample = (f"each step: leapfrog + full octree build of {N_BODIES} bodies + traversal of "
+              f"1/{int(round(1 / frac))} of the bodies (strided) scaled to all bodies")
+    line = {"impl": "reference", "metric": "bh_steps_per_s_1M_fp64_theta0.5", "value": value,
+            "unit": "steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "barnes-hut fp64 theta=0.5, 1,048,576-body heliocentric disc, "
+                                   "dt=1h, per-body opening rule",
+                       "bodies": N_BODIES, "theta": THETA},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------------------------
+# ours
+# ---------------------------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from nbody import generators
+    from nbody.lib import BHTree, Context, fma_peak
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(v: float) -> float:
+        if dist is None:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    ctx = Context(local)
+    d = generators.heliocentric_disc(N_BODIES, SEED)
+    n = N_BODIES
+    G = d["G"]
+    f64 = dict(dtype=torch.float64, device="cuda")
+    m = torch.as_tensor(d["m"], **f64)
+    pos = [torch.as_tensor(d[k], **f64) for k in ("x", "y", "z")]
+    vel = [torch.as_tensor(d[k], **f64) for k in ("vx", "vy", "vz")]
+    acc = [torch.zeros(n, **f64) for _ in range(3)]
+    vh = [torch.zeros(n, **f64) for _ in range(3)]
+    tree = BHTree(ctx, n, theta=THETA)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    trav_ev = []
+
+    def step(record_traversal=False):
+        ctx.kick_drift(vh, vel, pos, acc, DT)
+        tree.build(m, *pos, G)
+        if record_traversal:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+        tree.accel(*pos, *acc, G, EPS2, "theta", "f64")
+        if record_traversal:
+            e1.record()
+            trav_ev.append((e0, e1))
+        ctx.kick(vel, vh, acc, DT)
+
+    # initial accelerations (the reference's step 0)
+    tree.build(m, *pos, G)
+    tree.accel(*pos, *acc, G, EPS2, "theta", "f64")
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    step_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        step(record_traversal=True)
+        s1.record()
+        step_ms.append((s0, s1))
+    barrier()
+    clk = clocks.stop()
+    ctx.sync()
+    t_total = sum(a.elapsed_time(b) for a, b in step_ms) / 1e3
+    t_total = max_over_ranks(t_total)
+    ms_per_step = t_total / args.steps * 1e3
+    value = ws * args.steps / t_total
+    trav_ms = sum(a.elapsed_time(b) for a, b in trav_ev) / len(trav_ev)
+
+    # work model of the traversal on the current state
+    accepted, opened = tree.count_interactions(*pos, "theta")
+    flop = FLOP_ACCEPTED * accepted + FLOP_OPENED * opened
+    fp64_peak = fma_peak(ctx, fp64=True)
+    stats = tree.stats()
+
+    # build passes against HBM: algorithmic bytes of AABB + keys + sort + cells + centre of mass
+    build_ev = []
+    for _ in range(3):
+        flush.zero_()
+        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b0.record()
+        tree.build(m, *pos, G)
+        b1.record()
+        build_ev.append((b0, b1))
+    torch.cuda.synchronize()
+    build_ms = min(a.elapsed_time(b) for a, b in build_ev)
+    nodes = stats["node_count"]
+    build_bytes = (24 * n            # AABB reads x,y,z
+                   + 24 * n + 12 * n  # keys: read x,y,z; write key + id
+                   + 8 * 24 * n       # 8 radix passes: read + write key + id
+                   + 16 * n + 13 * n  # splits: read keys; write level, start, end (+mask)
+                   + 12 * n           # counts + scan
+                   + 24 * nodes       # emit: node level/first/last/skip/parent/body
+                   + 32 * n           # centre of mass: m, x, y, z per body
+                   + (68 + 80) * nodes)  # cell sums read/written + traversal records
+    hbm_peak, hbm_src = measured_hbm_peak()
+
+    # e2e: same step through the C ABI with the state in pinned host memory
+    host = {k: torch.as_tensor(d[k], dtype=torch.float64).pin_memory()
+            for k in ("m", "x", "y", "z", "vx", "vy", "vz")}
+    host_acc = [torch.zeros(n, dtype=torch.float64).pin_memory() for _ in range(3)]
+    h2d_arrays = [host["m"], host["x"], host["y"], host["z"], host["vx"], host["vy"], host["vz"]]
+    h2d_arrays += host_acc
+    dev_in = [m] + pos + vel + acc
+    e2e_steps = max(3, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for dv, hv in zip(dev_in, h2d_arrays):
+            dv.copy_(hv, non_blocking=True)
+        step()
+        for hv, dv in zip([host["x"], host["y"], host["z"], host["vx"], host["vy"], host["vz"]]
+                          + host_acc, pos + vel + acc):
+            hv.copy_(dv, non_blocking=True)
+        torch.cuda.synchronize()
+    t_e2e = max_over_ranks(time.perf_counter() - t0)
+    ctx.sync()
+    e2e_value = ws * e2e_steps / t_e2e
+
+    also = {}
+    if rank == 0 and not args.quick:
+        also = secondary_measurements(ctx, tree, m, pos, acc, G)
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        t_cpu, parts = cpu_bh_step_seconds(d, 1.0 / 16)
+        cpu = {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "one step: leapfrog + full octree build of 1,048,576 bodies + traversal of "
+                         "every 16th body scaled x16 (restated reference, OpenMP, all host cores)",
+               "build_s": parts["build_s"], "traversal_s": parts["traversal_s"]}
+
+    if rank == 0:
+        achieved = flop / (trav_ms * 1e-3)
+        line = {
+            "metric": "bh_steps_per_s_1M_fp64_theta0.5", "value": value, "unit": "steps/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "barnes-hut fp64 theta=0.5, 1,048,576-body heliocentric disc, "
+                                   "dt=1h, per-body opening rule (the reference's), "
+                                   "leapfrog + build + traversal per step",
+                       "bodies": n, "theta": THETA, "dt_days": DT, "eps2": EPS2,
+                       "l2": "256 MB buffer written before every timed step",
+                       "parallelism": f"replicas x{ws}"},
+            "e2e": {"value": e2e_value, "unit": "steps/s",
+                    "h2d_bytes_per_step": 8 * n * len(h2d_arrays),
+                    "d2h_bytes_per_step": 8 * n * 9},
+            "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+            "roofline": {"kernel": "bh_theta_f64_kernel (traversal)", "bound": "fp64",
+                         "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
+                         "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                         "traffic": load_traffic("bh_theta_f64_kernel"),
+                         "peak_source": "FP64 FMA throughput measured in this run "
+                                        "(nb_util_fma_peak)",
+                         "work": {"accepted_cells": accepted, "opened_cells": opened,
+                                  "flop_per_launch": flop, "ms_per_launch": trav_ms}},
+            "roofline_build": {"bound": "hbm", "achieved": build_bytes / (build_ms * 1e-3) / 1e9,
+                               "peak": hbm_peak, "unit": "GB/s",
+                               "frac": build_bytes / (build_ms * 1e-3) / 1e9 / hbm_peak,
+                               "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
+                               "ms_per_build": build_ms, "algorithmic_bytes": build_bytes,
+                               "traffic": load_traffic("bh_build")},
+            "tree": {"nodes": nodes, "max_depth": stats["max_depth"],
+                     "reference_layout_nodes": stats["ref_node_count"]},
+            "clocks": clk,
+            "cpu_baseline": cpu,
+            "also": also,
+        }
+        print(json.dumps(line), flush=True)
+    tree.close()
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def secondary_measurements(ctx, tree, m, pos, acc, G):
+    """Other configurations' throughput on the same GPU (short runs)."""
+    import torch
+
+    from nbody import generators
+    from nbody.lib import fma_peak
+
+    out = {}
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ctx.sync()
+        return e0.elapsed_time(e1) / reps
+
+    # FP32-pair Barnes-Hut (group rule) step at 1M on the same state
+    def bh32():
+        tree.build(m, *pos, G)
+        tree.accel(*pos, *acc, G, EPS2, "group", "f32c")
+    ms = timed(bh32, 10)
+    out["bh_f32c_group_theta0.5_1M"] = {"build_plus_traversal_ms": ms, "steps_per_s": 1e3 / ms}
+    fp32_peak = fma_peak(ctx, fp64=False)
+    # naive FP32-compensated, N = 262,144 Plummer (config 3 shape)
+    for name, n, prec, reps, kind in (("naive_f32c_plummer_262144", 262144, "f32c", 5, "plummer"),
+                                      ("naive_f64_disc_16384", 16384, "f64", 5, "disc")):
+        dd = generators.plummer(n, 1) if kind == "plummer" else generators.heliocentric_disc(n, 1)
+        t = {k: torch.as_tensor(dd[k], device="cuda") for k in ("m", "x", "y", "z")}
+        a = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+        eps2 = 1e-6 if kind == "plummer" else EPS2
+        ms = timed(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, dd["G"], eps2, prec),
+                   reps)
+        gp = n * n / (ms * 1e-3) / 1e9
+        peak = fp32_peak if prec == "f32c" else fma_peak(ctx, fp64=True)
+        out[name] = {"ms_per_eval": ms, "gpairs_per_s": gp, "tflops_20_per_pair": gp * 20 / 1e3,
+                     "frac_of_measured_fma_peak": gp * 20e9 / peak}
+    out["fp32_fma_peak_tflops"] = fp32_peak / 1e12
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="skip the secondary measurements")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -125,6 +125,111 @@ nb_status nb_energy(nb_ctx* ctx, const double* m, const double* x, const double*
 nb_status nb_aabb(nb_ctx* ctx, const double* x, const double* y, const double* z, uint32_t n,
                   double* out_dev, nb_stream_t stream);
 
+/* ---------------------------------------------------------------------------------------------
+ * Barnes-Hut.
+ * The tree is the reference's point-region octree over the cube AABB (one body per leaf, the
+ * octant rule of ParallelOctreeTopDownSubtrees.cpp:400-414 with its FP64 midpoint recurrence,
+ * so every body lands in the same octant at every level), stored compressed (no empty children,
+ * single-child chains folded into their deepest cell, which the reference's traversal accepts
+ * or opens identically) in DFS pre-order with skip links. Node sums are the reference's: children
+ * summed in octant order 0..7 in FP64 (BarnesHutOctree.cpp:304-311).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct nb_bh_params {
+    double theta;                 /* opening angle: a cell is accepted when edge/d < theta
+                                     (reference --theta, default 1.05) */
+    uint32_t storage_size_param;  /* reference --storage_size_param (default 16). The reference
+                                     needs storage_size_param*N node slots; this tree needs at
+                                     most 2N-1 and reports the reference's count in stats */
+    uint32_t stack_size_param;    /* reference --stack_size_param (default 16); the traversal
+                                     here is stackless, the value is recorded only */
+    int max_build_level;          /* reference --max_level_top_octree (default 7); the tree shape
+                                     and all results are independent of it */
+    int sort_bodies;              /* reference --sort_bodies (default 1): bodies are traversed in
+                                     tree order; results are independent of it */
+} nb_bh_params;
+
+typedef enum nb_opening {
+    NB_OPEN_THETA = 0,        /* the reference's per-body rule (BarnesHutAlgorithm.cpp:355-359):
+                                 accept if edge*rsqrt(d^2) < theta or the node is a body leaf;
+                                 contributions summed in the reference's DFS order */
+    NB_OPEN_THETA_GROUP = 1,  /* per group of 32 bodies adjacent in tree order: a cell is opened
+                                 for the whole group when any member's rule would open it
+                                 (never less accurate than NB_OPEN_THETA) */
+    NB_OPEN_LEARNED = 2       /* per (32-body group, cell) decision of a trained MLP, with the
+                                 group theta rule as fallback */
+} nb_opening;
+
+typedef struct nb_bh_tree nb_bh_tree;
+
+typedef struct nb_bh_stats {
+    uint32_t n;                   /* bodies of the last build */
+    uint32_t node_count;          /* nodes of the compressed tree (<= 2n-1) */
+    uint32_t max_depth;           /* deepest leaf level (root = 0) */
+    uint32_t ref_node_count;      /* nodes the reference's linearised octree holds for the same
+                                     bodies (nextFreeNodeID: 1 + 8 * internal cells) */
+    double aabb[7];               /* min x,y,z, max x,y,z, edge */
+} nb_bh_stats;
+
+/* Reference-layout export for parity checks (BarnesHutOctree.hpp:33-95). Caller-owned HOST
+ * arrays of capacity `capacity` nodes (octants: 8*capacity, plane o at octants[o*capacity]) and
+ * n bodies (sorted_bodies). Node ids: root 0, the 8 children of a split cell allocated together
+ * in the reference's slot order (octants 5,7,4,6,1,3,0,2), cells numbered breadth-first. */
+typedef struct nb_bh_ref_layout {
+    uint32_t capacity;
+    uint32_t node_count;          /* out */
+    uint32_t* octants;
+    double *edge, *min_x, *min_y, *min_z;
+    uint32_t* body_of_node;       /* n = empty or internal */
+    int* node_is_leaf;
+    double *sum_masses, *com_x, *com_y, *com_z;  /* com = mass-weighted numerators */
+    uint32_t* body_count;
+    uint32_t* sorted_bodies;      /* sortedBodiesInOrder (BarnesHutOctree.cpp:550-613) */
+} nb_bh_ref_layout;
+
+nb_status nb_bh_params_default(nb_bh_params* out);
+/* Allocates a tree for up to n_max bodies (device memory, ~0.5 KB per body). */
+nb_status nb_bh_tree_create(nb_ctx* ctx, uint32_t n_max, const nb_bh_params* params,
+                            nb_bh_tree** out);
+nb_status nb_bh_tree_destroy(nb_bh_tree* tree);
+nb_status nb_bh_tree_set_theta(nb_bh_tree* tree, double theta);
+
+/* Replaces BarnesHutOctree::buildOctree (BarnesHutOctree.hpp:102-103;
+ * ParallelOctreeTopDownSubtrees.cpp:15-93): AABB, octree, centre of mass, body order.
+ * G only scales the FP32 traversal records (masses stay in the caller's units). */
+nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* tree, const double* m, const double* x,
+                      const double* y, const double* z, uint32_t n, double G,
+                      nb_stream_t stream);
+
+/* Replaces BarnesHutAlgorithm::computeAccelerations (BarnesHutAlgorithm.hpp:43-46,
+ * BarnesHutAlgorithm.cpp:280-401) for the bodies of the last build (same x, y, z). */
+nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* tree, const double* x, const double* y,
+                      const double* z, double* ax, double* ay, double* az, double G, double eps2,
+                      nb_opening opening, nb_precision prec, nb_stream_t stream);
+
+/* Synchronous. */
+nb_status nb_bh_tree_stats(nb_bh_tree* tree, nb_bh_stats* out);
+nb_status nb_bh_export_ref_layout(nb_bh_tree* tree, nb_bh_ref_layout* out);
+/* Sorted body ids (tree DFS order) and per-body leaf depth, HOST arrays of n entries. */
+nb_status nb_bh_export_order(nb_bh_tree* tree, uint32_t* ids_in_dfs_order, uint32_t* leaf_level);
+
+/* Work model of a traversal: total cells accepted (interactions) into out_dev[0] and opened into
+ * out_dev[1] (DEVICE pointer to 2 uint64) under the per-body or the group theta rule. */
+nb_status nb_bh_count_interactions(nb_ctx* ctx, const nb_bh_tree* tree, const double* x,
+                                   const double* y, const double* z, nb_opening opening,
+                                   unsigned long long* out_dev, nb_stream_t stream);
+
+/* Synchronous FMA-throughput probe of the current GPU: FP64 (fp64 = 1) or FP32 flop/s (2 per FMA).
+ * The measured pipe peaks the pair and traversal kernels are reported against. */
+nb_status nb_util_fma_peak(nb_ctx* ctx, int fp64, double* flops_per_s);
+
+/* Building blocks exposed for tests: stable radix sort of (u64, u32) device pairs on bits
+ * [begin_bit, end_bit) and an exclusive scan of u32 device data (out has n+1 entries). These two
+ * allocate their temporaries with cudaMallocAsync on the stream. */
+nb_status nb_util_radix_sort_pairs(nb_ctx* ctx, uint64_t* keys, uint32_t* vals, uint32_t n,
+                                   int begin_bit, int end_bit, nb_stream_t stream);
+nb_status nb_util_exclusive_scan_u32(nb_ctx* ctx, const uint32_t* in, uint32_t* out, uint32_t n,
+                                     nb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,519 @@
+// nb_bh.cu -- Barnes-Hut octree build on the GPU (replaces BarnesHutOctree::buildOctree,
+// ParallelOctreeTopDownSubtrees.cpp:15-93, and its AABB / centre-of-mass / sortBodies passes).
+//
+// Pipeline (all on one stream, no host round trip):
+//  1. AABB with the reference's conventions (nb_integrate.cu).
+//  2. keys: per body the octant digit of every level from the reference's FP64 recurrence
+//     (mid = min + edge/2, strict compares, z below the midpoint selects bit 0; child min corner =
+//     parent min + child edge), mapped to the visit rank so that ascending keys are the
+//     reference's DFS pop order.
+//  3. stable LSD radix sort of (key, body id).
+//  4. bodies whose first 21 digits collide get their next 21 digits and are re-sorted in place.
+//  5. splits: adjacent sorted bodies share a prefix of L digits; the split belongs to the cell at
+//     level L containing both. Its cell range comes from galloping searches over the keys; the
+//     leftmost split of each cell ("first split") stands for the cell.
+//  6. DFS numbering: each sorted position p starts popc(mask[p]) internal cells plus its leaf;
+//     an exclusive scan gives every node its DFS pre-order index and skip link.
+//  7. bottom-up centre of mass: the last child to finish a cell sums the cell's children in
+//     octant order 0..7 (bit-identical to BarnesHutOctree.cpp:304-311).
+#include "nb_bh.cuh"
+#include "nb_sort.cuh"
+
+namespace nb {
+nb_status launch_aabb(nb_ctx* ctx, const double* x, const double* y, const double* z, uint32_t n,
+                      double* out_dev, cudaStream_t stream);
+}
+
+namespace {
+
+constexpr int BH_THREADS = 256;
+constexpr uint32_t RUN_LIMIT = 1u << 14;  // longest run of equal first key words we re-sort
+
+// Octant digits of levels [word*21, word*21+21) for a body (FP64 recurrence, no contraction).
+__device__ uint64_t key_word(const double* __restrict__ box, double px, double py, double pz,
+                             int word) {
+    double mnx = box[0], mny = box[1], mnz = box[2], e = box[6];
+    uint64_t key = 0;
+    const int first = word * NB_KEY_LEVELS, last = first + NB_KEY_LEVELS;
+    for (int L = 0; L < last; ++L) {
+        const double ce = e / 2;
+        const double midx = __dadd_rn(mnx, ce);
+        const double midy = __dadd_rn(mny, ce);
+        const double midz = __dadd_rn(mnz, ce);
+        const bool up = py > midy, rt = px > midx, bk = pz < midz;
+        if (L >= first)
+            key = (key << 3) | nb_visit_of_octant((uint32_t)up * 4u + (uint32_t)rt * 2u + (uint32_t)bk);
+        if (rt) mnx = midx;
+        if (up) mny = midy;
+        if (!bk) mnz = midz;
+        e = ce;
+    }
+    return key;
+}
+
+__global__ void keys_kernel(const double* __restrict__ x, const double* __restrict__ y,
+                            const double* __restrict__ z, uint32_t n,
+                            const double* __restrict__ box, uint64_t* __restrict__ key0,
+                            uint32_t* __restrict__ ids) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    key0[i] = key_word(box, x[i], y[i], z[i], 0);
+    ids[i] = i;
+}
+
+// Runs of equal first words: compute the second word and insertion-sort the run (stable).
+__global__ void runs_fixup_kernel(const double* __restrict__ x, const double* __restrict__ y,
+                                  const double* __restrict__ z, uint32_t n,
+                                  const double* __restrict__ box, const uint64_t* __restrict__ key0,
+                                  uint64_t* __restrict__ key1, uint32_t* __restrict__ ids,
+                                  uint32_t* __restrict__ err) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p + 1 >= n) return;
+    const uint64_t k = key0[p];
+    if (key0[p + 1] != k) return;
+    if (p > 0 && key0[p - 1] == k) return;
+    uint32_t r = 2;
+    while (p + r < n && key0[p + r] == k && r < RUN_LIMIT) ++r;
+    if (p + r < n && key0[p + r] == k) {
+        atomicOr(err, NB_DEVERR_DEPTH);
+        return;
+    }
+    for (uint32_t q = p; q < p + r; ++q) {
+        const uint32_t b = ids[q];
+        key1[q] = key_word(box, x[b], y[b], z[b], 1);
+    }
+    for (uint32_t q = p + 1; q < p + r; ++q) {  // insertion sort, stable
+        const uint64_t kk = key1[q];
+        const uint32_t bb = ids[q];
+        uint32_t s = q;
+        while (s > p && key1[s - 1] > kk) {
+            key1[s] = key1[s - 1];
+            ids[s] = ids[s - 1];
+            --s;
+        }
+        key1[s] = kk;
+        ids[s] = bb;
+    }
+}
+
+// Number of leading octal digits two sorted positions share (0 .. 42).
+__device__ __forceinline__ int shared_digits(const uint64_t* __restrict__ key0,
+                                             const uint64_t* __restrict__ key1, uint32_t p,
+                                             uint32_t q) {
+    const uint64_t a = key0[p], b = key0[q];
+    if (a != b) return (__clzll((long long)(a ^ b)) - 1) / 3;
+    const uint64_t c = key1[p], d = key1[q];
+    if (c != d) return NB_KEY_LEVELS + (__clzll((long long)(c ^ d)) - 1) / 3;
+    return 2 * NB_KEY_LEVELS;
+}
+
+__global__ void splits_kernel(const uint64_t* __restrict__ key0, const uint64_t* __restrict__ key1,
+                              uint32_t n, uint8_t* __restrict__ split_level,
+                              uint32_t* __restrict__ split_start, uint32_t* __restrict__ split_end,
+                              unsigned long long* __restrict__ mask, uint32_t* __restrict__ err) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j + 1 >= n) return;
+    int L = shared_digits(key0, key1, j, j + 1);
+    if (L >= 2 * NB_KEY_LEVELS) {
+        atomicOr(err, NB_DEVERR_DEPTH);
+        L = 2 * NB_KEY_LEVELS - 1;
+    }
+    split_level[j] = (uint8_t)L;
+    // leftmost a <= j with shared_digits(a, j) >= L (galloping, then bisection)
+    long long good = j, bad = -1;
+    for (long long step = 1;; step <<= 1) {
+        const long long c = good - step;
+        if (c < 0) break;
+        if (shared_digits(key0, key1, (uint32_t)c, j) >= L) {
+            good = c;
+        } else {
+            bad = c;
+            break;
+        }
+    }
+    while (good - bad > 1) {
+        const long long mid = bad + (good - bad) / 2;
+        if (shared_digits(key0, key1, (uint32_t)mid, j) >= L) good = mid; else bad = mid;
+    }
+    const uint32_t a = (uint32_t)good;
+    split_start[j] = a;
+    const bool first = (a == j) || shared_digits(key0, key1, a, j) > L;
+    if (!first) {
+        split_end[j] = NB_NONE;
+        return;
+    }
+    // rightmost b >= j+1 with shared_digits(j, b) >= L
+    long long g2 = j + 1, b2 = n;
+    for (long long step = 1;; step <<= 1) {
+        const long long c = g2 + step;
+        if (c >= (long long)n) break;
+        if (shared_digits(key0, key1, j, (uint32_t)c) >= L) {
+            g2 = c;
+        } else {
+            b2 = c;
+            break;
+        }
+    }
+    while (b2 - g2 > 1) {
+        const long long mid = g2 + (b2 - g2) / 2;
+        if (shared_digits(key0, key1, j, (uint32_t)mid) >= L) g2 = mid; else b2 = mid;
+    }
+    split_end[j] = (uint32_t)g2;
+    atomicOr(&mask[a], 1ull << L);
+}
+
+__global__ void count_kernel(const unsigned long long* __restrict__ mask, uint32_t n,
+                             uint32_t* __restrict__ cnt) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) cnt[p] = __popcll(mask[p]) + 1;
+}
+
+__device__ __forceinline__ uint32_t node_index(const uint32_t* __restrict__ base,
+                                               const unsigned long long* __restrict__ mask,
+                                               uint32_t start, int level) {
+    return base[start] + __popcll(mask[start] & ((1ull << level) - 1ull));
+}
+
+// Parent of the node covering sorted positions [a, b]: the cell at level max(dl, dr) holding the
+// neighbouring split (dl = level of split a-1, dr = level of split b, -1 when absent).
+__device__ __forceinline__ uint32_t parent_of(uint32_t a, uint32_t b, int dl, int dr,
+                                              const uint8_t* __restrict__ split_level,
+                                              const uint32_t* __restrict__ split_start,
+                                              const uint32_t* __restrict__ base,
+                                              const unsigned long long* __restrict__ mask) {
+    if (dl < 0 && dr < 0) return NB_NONE;
+    const uint32_t s = dl >= dr ? a - 1 : b;
+    return node_index(base, mask, split_start[s], split_level[s]);
+}
+
+__global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
+                            const uint8_t* __restrict__ split_level,
+                            const uint32_t* __restrict__ split_start,
+                            const uint32_t* __restrict__ split_end,
+                            const unsigned long long* __restrict__ mask,
+                            const uint32_t* __restrict__ base, uint8_t* __restrict__ node_level,
+                            uint32_t* __restrict__ node_first, uint32_t* __restrict__ node_last,
+                            uint32_t* __restrict__ node_skip, uint32_t* __restrict__ node_parent,
+                            uint32_t* __restrict__ node_body, uint32_t* __restrict__ node_nchild,
+                            uint32_t* __restrict__ info) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    if (p == 0) info[0] = base[n];
+    {  // leaf of the body at sorted position p
+        const int dl = p > 0 ? (int)split_level[p - 1] : -1;
+        const int dr = p + 1 < n ? (int)split_level[p] : -1;
+        const uint32_t idx = base[p] + __popcll(mask[p]);
+        node_level[idx] = (uint8_t)(max(dl, dr) + 1);
+        node_first[idx] = p;
+        node_last[idx] = p;
+        node_skip[idx] = base[p + 1];
+        node_body[idx] = ids[p];
+        const uint32_t par = parent_of(p, p, dl, dr, split_level, split_start, base, mask);
+        node_parent[idx] = par;
+        if (par != NB_NONE) atomicAdd(&node_nchild[par], 1u);
+    }
+    if (p + 1 < n && split_end[p] != NB_NONE) {  // internal cell whose first split is p
+        const uint32_t a = split_start[p], b = split_end[p];
+        const int L = split_level[p];
+        const uint32_t idx = node_index(base, mask, a, L);
+        node_level[idx] = (uint8_t)L;
+        node_first[idx] = a;
+        node_last[idx] = b;
+        node_skip[idx] = base[b + 1];
+        node_body[idx] = NB_NONE;
+        const int dl = a > 0 ? (int)split_level[a - 1] : -1;
+        const int dr = b + 1 < n ? (int)split_level[b] : -1;
+        const uint32_t par = parent_of(a, b, dl, dr, split_level, split_start, base, mask);
+        node_parent[idx] = par;
+        if (par != NB_NONE) atomicAdd(&node_nchild[par], 1u);
+    }
+}
+
+__device__ __forceinline__ uint32_t digit_at(const uint64_t* __restrict__ key0,
+                                             const uint64_t* __restrict__ key1, uint32_t q, int L) {
+    if (L < NB_KEY_LEVELS) return (uint32_t)(key0[q] >> (60 - 3 * L)) & 7u;
+    return (uint32_t)(key1[q] >> (60 - 3 * (L - NB_KEY_LEVELS))) & 7u;
+}
+
+struct ComArgs {
+    uint32_t n;
+    const double *m, *x, *y, *z;
+    const double* box;
+    double G;
+    const uint64_t *key0, *key1;
+    const uint32_t* ids;
+    const unsigned long long* mask;
+    const uint32_t* base;
+    const uint8_t* node_level;
+    const uint32_t *node_first, *node_skip, *node_parent, *node_body, *node_nchild;
+    uint32_t *node_arrive, *node_count;
+    double *comx, *comy, *comz, *mass;
+    NodeRec64* rec64;
+    NodeRec32* rec32;
+};
+
+__device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double cy, double cz,
+                              double sm, int level, uint32_t skip, uint32_t body) {
+    const double edge = ldexp(A.box[6], -level);
+    NodeRec64 r;
+    r.cx = __ddiv_rn(cx, sm);
+    r.cy = __ddiv_rn(cy, sm);
+    r.cz = __ddiv_rn(cz, sm);
+    r.mass = sm;
+    r.edge = edge;
+    r.skip = skip;
+    r.body = body;
+    A.rec64[idx] = r;
+    NodeRec32 q;
+    if (sm != 0) {
+        const double ox = A.box[0] + A.box[6] / 2, oy = A.box[1] + A.box[6] / 2,
+                     oz = A.box[2] + A.box[6] / 2;
+        q.cx = (float)(r.cx - ox);
+        q.cy = (float)(r.cy - oy);
+        q.cz = (float)(r.cz - oz);
+    } else {  // massless cell: far away, contributes exactly 0
+        q.cx = q.cy = q.cz = 1e30f;
+    }
+    q.gm = (float)(A.G * sm);
+    q.edge2 = (float)(edge * edge);
+    q.skip = skip;
+    q.body = body;
+    q.level = (uint32_t)level;
+    A.rec32[idx] = q;
+}
+
+__global__ void com_kernel(ComArgs A) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= A.n) return;
+    const uint32_t idx = A.base[p] + __popcll(A.mask[p]);
+    const uint32_t b = A.ids[p];
+    const double mb = A.m[b];
+    const double cx = __dmul_rn(A.x[b], mb), cy = __dmul_rn(A.y[b], mb), cz = __dmul_rn(A.z[b], mb);
+    A.comx[idx] = cx;
+    A.comy[idx] = cy;
+    A.comz[idx] = cz;
+    A.mass[idx] = mb;
+    A.node_count[idx] = 1;
+    write_records(A, idx, cx, cy, cz, mb, A.node_level[idx], A.node_skip[idx], b);
+    uint32_t cur = A.node_parent[idx];
+    while (cur != NB_NONE) {
+        __threadfence();
+        if (atomicAdd(&A.node_arrive[cur], 1u) != A.node_nchild[cur] - 1u) return;
+        __threadfence();
+        const int L = A.node_level[cur];
+        uint32_t slot[8];
+#pragma unroll
+        for (int o = 0; o < 8; ++o) slot[o] = NB_NONE;
+        const uint32_t end = A.node_skip[cur];
+        uint32_t c = cur + 1;
+        for (int k = 0; k < 8 && c < end; ++k) {
+            slot[nb_octant_of_visit(digit_at(A.key0, A.key1, A.node_first[c], L))] = c;
+            c = A.node_skip[c];
+        }
+        double sx = 0, sy = 0, sz = 0, sm = 0;
+        uint32_t count = 0;
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+            const uint32_t ch = slot[o];
+            if (ch == NB_NONE) continue;
+            sx = __dadd_rn(sx, __ldcg(&A.comx[ch]));
+            sy = __dadd_rn(sy, __ldcg(&A.comy[ch]));
+            sz = __dadd_rn(sz, __ldcg(&A.comz[ch]));
+            sm = __dadd_rn(sm, __ldcg(&A.mass[ch]));
+            count += __ldcg(&A.node_count[ch]);
+        }
+        A.comx[cur] = sx;
+        A.comy[cur] = sy;
+        A.comz[cur] = sz;
+        A.mass[cur] = sm;
+        A.node_count[cur] = count;
+        write_records(A, cur, sx, sy, sz, sm, L, end, NB_NONE);
+        cur = A.node_parent[cur];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// allocation
+// ---------------------------------------------------------------------------------------------
+struct Carver {
+    char* base = nullptr;
+    size_t off = 0;
+    template <typename T>
+    T* take(size_t count) {
+        off = (off + 255) & ~(size_t)255;
+        T* p = (T*)(base + off);
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+void carve(nb_bh_tree* t, Carver& c) {
+    const size_t n = t->n_max, cap = t->node_cap;
+    t->box = c.take<double>(16);
+    t->info = c.take<uint32_t>(16);
+    t->key0 = c.take<uint64_t>(n);
+    t->key1 = c.take<uint64_t>(n);
+    t->key_alt = c.take<uint64_t>(n);
+    t->ids = c.take<uint32_t>(n);
+    t->ids_alt = c.take<uint32_t>(n);
+    t->split_level = c.take<uint8_t>(n);
+    t->split_start = c.take<uint32_t>(n);
+    t->split_end = c.take<uint32_t>(n);
+    t->mask = c.take<uint64_t>(n);
+    t->cnt = c.take<uint32_t>(n + 1);
+    t->base = c.take<uint32_t>(n + 1);
+    t->sort_temp = c.take<char>(nb::radix_temp_bytes((uint32_t)n));
+    t->scan_temp = c.take<uint32_t>(nb::scan_temp_bytes((uint32_t)n + 1) / 4 + 16);
+    t->node_level = c.take<uint8_t>(cap);
+    t->node_first = c.take<uint32_t>(cap);
+    t->node_last = c.take<uint32_t>(cap);
+    t->node_skip = c.take<uint32_t>(cap);
+    t->node_parent = c.take<uint32_t>(cap);
+    t->node_body = c.take<uint32_t>(cap);
+    t->node_nchild = c.take<uint32_t>(cap);
+    t->node_arrive = c.take<uint32_t>(cap);
+    t->node_count = c.take<uint32_t>(cap);
+    t->node_comx = c.take<double>(cap);
+    t->node_comy = c.take<double>(cap);
+    t->node_comz = c.take<double>(cap);
+    t->node_mass = c.take<double>(cap);
+    t->rec64 = c.take<NodeRec64>(cap);
+    t->rec32 = c.take<NodeRec32>(cap);
+}
+
+}  // namespace
+
+extern "C" {
+
+nb_status nb_bh_params_default(nb_bh_params* out) {
+    if (!out) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_params_default: null pointer");
+    out->theta = 1.05;  // Configuration.cpp:18
+    out->storage_size_param = 16;
+    out->stack_size_param = 16;
+    out->max_build_level = 7;
+    out->sort_bodies = 1;
+    return NB_OK;
+}
+
+nb_status nb_bh_tree_create(nb_ctx* ctx, uint32_t n_max, const nb_bh_params* params,
+                            nb_bh_tree** out) {
+    NB_CHECK_CTX(ctx);
+    if (!out) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_tree_create: null output");
+    if (n_max == 0 || n_max > (1u << 27))
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_tree_create: n_max = %u out of range", n_max);
+    nb_bh_tree* t = new nb_bh_tree();
+    t->n_max = n_max;
+    t->node_cap = 2 * n_max;
+    t->device = ctx->device;
+    if (params) {
+        t->params = *params;
+    } else {
+        nb_bh_params_default(&t->params);
+    }
+    Carver sizing;
+    carve(t, sizing);
+    void* mem = nullptr;
+    cudaError_t e = cudaMalloc(&mem, sizing.off + 256);
+    if (e != cudaSuccess) {
+        delete t;
+        return nb::cuda_error(e, "nb_bh_tree_create");
+    }
+    Carver real;
+    real.base = (char*)mem;
+    carve(t, real);
+    // the carve order puts box first: its address is the allocation base (freed in destroy)
+    *out = t;
+    return NB_OK;
+}
+
+nb_status nb_bh_tree_destroy(nb_bh_tree* t) {
+    if (!t) return NB_OK;
+    if (t->box) cudaFree(t->box);
+    delete t;
+    return NB_OK;
+}
+
+nb_status nb_bh_tree_set_theta(nb_bh_tree* t, double theta) {
+    if (!t) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_tree_set_theta: null tree");
+    if (!(theta >= 0)) return nb::set_error(NB_ERR_INVALID_ARG, "theta must be >= 0");
+    t->params.theta = theta;
+    return NB_OK;
+}
+
+nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double* x,
+                      const double* y, const double* z, uint32_t n, double G,
+                      nb_stream_t stream_) {
+    NB_CHECK_CTX(ctx);
+    if (!t) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_build: null tree");
+    if (!m || !x || !y || !z) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_build: null array");
+    if (n == 0 || n > t->n_max)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_build: n = %u (tree capacity %u)", n, t->n_max);
+    cudaStream_t s = (cudaStream_t)stream_;
+    t->built = false;
+    t->n = n;
+    t->G = G;
+    const int grid = nb::ceil_div(n, BH_THREADS);
+    NB_TRY(nb::launch_aabb(ctx, x, y, z, n, t->box, s));
+    keys_kernel<<<grid, BH_THREADS, 0, s>>>(x, y, z, n, t->box, t->key0, t->ids);
+    NB_TRY(nb::check_launch("keys_kernel"));
+    int in_alt = 0;
+    NB_TRY(nb::radix_sort_pairs(t->key0, t->ids, t->key_alt, t->ids_alt, n, 0, 3 * NB_KEY_LEVELS,
+                                t->sort_temp, s, &in_alt));
+    if (in_alt) {  // an odd number of passes leaves the result in the alternate buffers
+        NB_CUDA_TRY(cudaMemcpyAsync(t->key0, t->key_alt, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
+        NB_CUDA_TRY(cudaMemcpyAsync(t->ids, t->ids_alt, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    }
+    NB_CUDA_TRY(cudaMemsetAsync(t->key1, 0, (size_t)n * 8, s));
+    runs_fixup_kernel<<<grid, BH_THREADS, 0, s>>>(x, y, z, n, t->box, t->key0, t->key1, t->ids,
+                                                  ctx->dev_error);
+    NB_TRY(nb::check_launch("runs_fixup_kernel"));
+    NB_CUDA_TRY(cudaMemsetAsync(t->mask, 0, (size_t)n * 8, s));
+    splits_kernel<<<grid, BH_THREADS, 0, s>>>(t->key0, t->key1, n, t->split_level, t->split_start,
+                                              t->split_end, (unsigned long long*)t->mask,
+                                              ctx->dev_error);
+    NB_TRY(nb::check_launch("splits_kernel"));
+    count_kernel<<<grid, BH_THREADS, 0, s>>>((const unsigned long long*)t->mask, n, t->cnt);
+    NB_TRY(nb::check_launch("count_kernel"));
+    NB_TRY(nb::exclusive_scan_u32(t->cnt, t->base, n, 1, t->scan_temp, s));
+    const size_t nodes_max = 2 * (size_t)n;
+    NB_CUDA_TRY(cudaMemsetAsync(t->node_nchild, 0, nodes_max * 4, s));
+    NB_CUDA_TRY(cudaMemsetAsync(t->node_arrive, 0, nodes_max * 4, s));
+    emit_kernel<<<grid, BH_THREADS, 0, s>>>(n, t->ids, t->split_level, t->split_start, t->split_end,
+                                            (const unsigned long long*)t->mask, t->base,
+                                            t->node_level, t->node_first, t->node_last, t->node_skip,
+                                            t->node_parent, t->node_body, t->node_nchild, t->info);
+    NB_TRY(nb::check_launch("emit_kernel"));
+    ComArgs A;
+    A.n = n;
+    A.m = m;
+    A.x = x;
+    A.y = y;
+    A.z = z;
+    A.box = t->box;
+    A.G = G;
+    A.key0 = t->key0;
+    A.key1 = t->key1;
+    A.ids = t->ids;
+    A.mask = (const unsigned long long*)t->mask;
+    A.base = t->base;
+    A.node_level = t->node_level;
+    A.node_first = t->node_first;
+    A.node_skip = t->node_skip;
+    A.node_parent = t->node_parent;
+    A.node_body = t->node_body;
+    A.node_nchild = t->node_nchild;
+    A.node_arrive = t->node_arrive;
+    A.node_count = t->node_count;
+    A.comx = t->node_comx;
+    A.comy = t->node_comy;
+    A.comz = t->node_comz;
+    A.mass = t->node_mass;
+    A.rec64 = t->rec64;
+    A.rec32 = t->rec32;
+    com_kernel<<<grid, BH_THREADS, 0, s>>>(A);
+    NB_TRY(nb::check_launch("com_kernel"));
+    t->built = true;
+    return NB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+// nb_bh.cuh -- Barnes-Hut octree object shared by the build, traversal and export units.
+//
+// Layout in HBM (n_max bodies, at most 2*n_max - 1 nodes):
+//  per body (sorted order): key0/key1 (u64, 21 octal digits each), ids (u32 body id)
+//  per adjacent pair of sorted bodies ("split"): level (u8), start of its node (u32), end (u32)
+//  per sorted position: mask (u64, levels of internal nodes whose range starts here), base (u32,
+//    DFS index of the first node starting here)
+//  per node (DFS pre-order, children in the reference's visit order 2,0,3,1,6,4,7,5):
+//    level, first/last sorted position, skip (DFS index after the subtree), parent, body,
+//    child count, centre-of-mass numerators and mass (FP64, the reference's sums), and the
+//    traversal records rec64 (FP64 centre, mass, edge, skip, body: 48 B) and rec32 (FP32 centre
+//    relative to the box centre, G*mass, edge^2, skip, body: 32 B).
+#pragma once
+#include "nb_internal.cuh"
+
+constexpr uint32_t NB_NONE = 0xffffffffu;
+constexpr int NB_KEY_LEVELS = 21;  // octal digits per 64-bit key word (bits 62..0)
+
+struct __align__(16) NodeRec64 {
+    double cx, cy, cz, mass;
+    double edge;
+    uint32_t skip, body;  // body = NB_NONE for internal nodes
+};
+
+struct __align__(16) NodeRec32 {
+    float cx, cy, cz, gm;  // centre relative to the box centre, G * mass
+    float edge2;           // edge^2
+    uint32_t skip, body, level;
+};
+
+struct nb_bh_tree {
+    uint32_t n_max = 0;
+    uint32_t n = 0;
+    uint32_t node_cap = 0;
+    nb_bh_params params{};
+    bool built = false;
+    double G = 0;
+    int device = 0;
+
+    double* box = nullptr;  // [0..6] AABB (min xyz, max xyz, edge), [7..9] box centre
+    uint32_t* info = nullptr;  // [0] node count (copy of base[n])
+
+    uint64_t *key0 = nullptr, *key1 = nullptr, *key_alt = nullptr;
+    uint32_t *ids = nullptr, *ids_alt = nullptr;
+    uint8_t* split_level = nullptr;
+    uint32_t *split_start = nullptr, *split_end = nullptr;
+    uint64_t* mask = nullptr;
+    uint32_t *cnt = nullptr, *base = nullptr;
+    void* sort_temp = nullptr;
+    uint32_t* scan_temp = nullptr;
+
+    uint8_t* node_level = nullptr;
+    uint32_t *node_first = nullptr, *node_last = nullptr, *node_skip = nullptr;
+    uint32_t *node_parent = nullptr, *node_body = nullptr, *node_nchild = nullptr;
+    uint32_t *node_arrive = nullptr, *node_count = nullptr;
+    double *node_comx = nullptr, *node_comy = nullptr, *node_comz = nullptr, *node_mass = nullptr;
+    NodeRec64* rec64 = nullptr;
+    NodeRec32* rec32 = nullptr;
+};
+
+// Digit maps between the reference's octant index o = 4*(y>mid) + 2*(x>mid) + (z<mid) and the
+// visit rank t (the reference pushes children 5,7,4,6,1,3,0,2 and pops 2,0,3,1,6,4,7,5).
+__host__ __device__ __forceinline__ uint32_t nb_visit_of_octant(uint32_t o) {
+    return (o & 4u) | ((o & 1u) << 1) | (((o >> 1) & 1u) ^ 1u);
+}
+__host__ __device__ __forceinline__ uint32_t nb_octant_of_visit(uint32_t t) {
+    return (t & 4u) | ((t & 2u) >> 1) | (((~t) & 1u) << 1);
+}

@@ -1,0 +1,408 @@
+// nb_bh_traverse.cu -- Barnes-Hut accelerations over the DFS-ordered octree
+// (replaces BarnesHutAlgorithm::computeAccelerations, BarnesHutAlgorithm.cpp:280-401).
+//
+// Nodes are stored in the order the reference's stack pops them (DFS pre-order, children in
+// visit order 2,0,3,1,6,4,7,5), each with a skip link to the first node after its subtree.
+// "Accept" (or skip) continues at the skip link and "open" continues at the next node, so a
+// traversal needs no stack at all and visits nodes in exactly the reference's order.
+//
+//  * per-body rule (NB_OPEN_THETA): the 32 lanes of a warp hold 32 bodies adjacent in tree order,
+//    each with its own position in the DFS sequence. Every iteration the warp takes the smallest
+//    position (__reduce_min_sync) and the lanes sitting on it evaluate that node -- one broadcast
+//    load -- and advance by their own decision. Each body sees the reference's sequence of
+//    accepted nodes in the reference's order.
+//  * group rule (NB_OPEN_THETA_GROUP): the warp walks one sequence; a cell is opened when any
+//    lane's rule opens it, otherwise all lanes accept it -- no divergence.
+#include "nb_bh.cuh"
+
+namespace {
+
+constexpr int TR_THREADS = 128;
+
+enum Mode { IEEE64 = 0, FAST64 = 1, F32 = 2 };
+
+template <int MODE>
+struct Arith;
+
+template <>
+struct Arith<IEEE64> {
+    __device__ static double sub(double a, double b) { return __dsub_rn(a, b); }
+    __device__ static double norm2(double a, double b, double c) {
+        return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+    }
+    __device__ static double rsqrt(double v) { return __ddiv_rn(1.0, __dsqrt_rn(v)); }
+    __device__ static double mul(double a, double b) { return __dmul_rn(a, b); }
+    __device__ static double add(double a, double b) { return __dadd_rn(a, b); }
+    // acc += m * (d * inv), rounded as the reference writes it
+    __device__ static double accum(double acc, double m, double d, double inv) {
+        return __dadd_rn(acc, __dmul_rn(m, __dmul_rn(d, inv)));
+    }
+};
+
+template <>
+struct Arith<FAST64> {
+    __device__ static double sub(double a, double b) { return a - b; }
+    __device__ static double norm2(double a, double b, double c) { return fma(a, a, fma(b, b, c * c)); }
+    __device__ static double rsqrt(double v) { return nb_rsqrt_f64(v); }
+    __device__ static double mul(double a, double b) { return a * b; }
+    __device__ static double add(double a, double b) { return a + b; }
+    __device__ static double accum(double acc, double m, double d, double inv) {
+        return fma(m * inv, d, acc);
+    }
+};
+
+// Per-body reference rule, FP64 (IEEE64 bit-identical to the host evaluation; FAST64 with FMAs).
+template <int MODE>
+__global__ void __launch_bounds__(TR_THREADS)
+bh_theta_f64_kernel(const NodeRec64* __restrict__ rec, const uint32_t* __restrict__ info,
+                    const uint32_t* __restrict__ ids, const double* __restrict__ x,
+                    const double* __restrict__ y, const double* __restrict__ z, uint32_t n,
+                    double theta, double eps2, double G, double* __restrict__ ax,
+                    double* __restrict__ ay, double* __restrict__ az) {
+    using A = Arith<MODE>;
+    const uint32_t p = blockIdx.x * TR_THREADS + threadIdx.x;
+    const bool valid = p < n;
+    const uint32_t nn = info[0];
+    const uint32_t me = valid ? ids[p] : NB_NONE;
+    double px = 0, py = 0, pz = 0;
+    if (valid) {
+        px = x[me];
+        py = y[me];
+        pz = z[me];
+    }
+    double acx = 0, acy = 0, acz = 0;
+    uint32_t kl = valid ? 0u : nn;
+    for (;;) {
+        const uint32_t k = __reduce_min_sync(0xffffffffu, kl);
+        if (k >= nn) break;
+        if (kl != k) continue;
+        const NodeRec64 r = rec[k];
+        if (r.mass != 0 && r.body != me) {  // BarnesHutAlgorithm.cpp:349
+            const double dx = A::sub(r.cx, px), dy = A::sub(r.cy, py), dz = A::sub(r.cz, pz);
+            const double d2 = A::norm2(dx, dy, dz);
+            const double cur = A::mul(r.edge, A::rsqrt(d2));  // :355-357
+            if (cur < theta || r.body != NB_NONE) {           // :359
+                double den = A::add(d2, eps2);
+                den = A::mul(A::mul(den, den), den);
+                const double inv = A::rsqrt(den);
+                acx = A::accum(acx, r.mass, dx, inv);
+                acy = A::accum(acy, r.mass, dy, inv);
+                acz = A::accum(acz, r.mass, dz, inv);
+                kl = r.skip;
+            } else {
+                kl = k + 1;
+            }
+        } else {
+            kl = r.skip;
+        }
+    }
+    if (valid) {
+        ax[me] = A::mul(acx, G);
+        ay[me] = A::mul(acy, G);
+        az[me] = A::mul(acz, G);
+    }
+}
+
+// Per-body reference rule with FP32 pair math and compensated accumulation.
+__global__ void __launch_bounds__(TR_THREADS)
+bh_theta_f32_kernel(const NodeRec32* __restrict__ rec, const uint32_t* __restrict__ info,
+                    const uint32_t* __restrict__ ids, const double* __restrict__ x,
+                    const double* __restrict__ y, const double* __restrict__ z,
+                    const double* __restrict__ box, uint32_t n, float theta, float eps2,
+                    double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az) {
+    const uint32_t p = blockIdx.x * TR_THREADS + threadIdx.x;
+    const bool valid = p < n;
+    const uint32_t nn = info[0];
+    const uint32_t me = valid ? ids[p] : NB_NONE;
+    const double ox = box[0] + box[6] / 2, oy = box[1] + box[6] / 2, oz = box[2] + box[6] / 2;
+    float px = 0, py = 0, pz = 0;
+    if (valid) {
+        px = (float)(x[me] - ox);
+        py = (float)(y[me] - oy);
+        pz = (float)(z[me] - oz);
+    }
+    float hx = 0, hy = 0, hz = 0, lx = 0, ly = 0, lz = 0;
+    uint32_t kl = valid ? 0u : nn;
+    const float theta2 = theta * theta;
+    for (;;) {
+        const uint32_t k = __reduce_min_sync(0xffffffffu, kl);
+        if (k >= nn) break;
+        if (kl != k) continue;
+        const NodeRec32 r = rec[k];
+        if (r.gm != 0 && r.body != me) {
+            const float dx = r.cx - px, dy = r.cy - py, dz = r.cz - pz;
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            if (r.body != NB_NONE || r.edge2 < theta2 * d2) {
+                const float inv = nb_rsqrt_f32(d2 + eps2);
+                const float s = r.gm * inv * inv * inv;
+                // TwoSum of each term into (h, l)
+                const float tx = dx * s, ty = dy * s, tz = dz * s;
+                float sh = hx + tx, bp = sh - hx;
+                lx += (hx - (sh - bp)) + (tx - bp);
+                hx = sh;
+                sh = hy + ty;
+                bp = sh - hy;
+                ly += (hy - (sh - bp)) + (ty - bp);
+                hy = sh;
+                sh = hz + tz;
+                bp = sh - hz;
+                lz += (hz - (sh - bp)) + (tz - bp);
+                hz = sh;
+                kl = r.skip;
+            } else {
+                kl = k + 1;
+            }
+        } else {
+            kl = r.skip;
+        }
+    }
+    if (valid) {
+        ax[me] = (double)hx + (double)lx;
+        ay[me] = (double)hy + (double)ly;
+        az[me] = (double)hz + (double)lz;
+    }
+}
+
+// Group rule, FP64.
+__global__ void __launch_bounds__(TR_THREADS)
+bh_group_f64_kernel(const NodeRec64* __restrict__ rec, const uint32_t* __restrict__ info,
+                    const uint32_t* __restrict__ ids, const double* __restrict__ x,
+                    const double* __restrict__ y, const double* __restrict__ z, uint32_t n,
+                    double theta, double eps2, double G, double* __restrict__ ax,
+                    double* __restrict__ ay, double* __restrict__ az) {
+    const uint32_t p = blockIdx.x * TR_THREADS + threadIdx.x;
+    const bool valid = p < n;
+    const uint32_t nn = info[0];
+    const uint32_t me = valid ? ids[p] : NB_NONE;
+    double px = 0, py = 0, pz = 0;
+    if (valid) {
+        px = x[me];
+        py = y[me];
+        pz = z[me];
+    }
+    const double theta2 = theta * theta;
+    double acx = 0, acy = 0, acz = 0;
+    uint32_t k = 0;
+    while (k < nn) {
+        const NodeRec64 r = rec[k];
+        const double dx = r.cx - px, dy = r.cy - py, dz = r.cz - pz;
+        const double d2 = fma(dx, dx, fma(dy, dy, dz * dz));
+        const bool open = valid && r.body == NB_NONE && r.mass != 0 && r.edge * r.edge >= theta2 * d2;
+        if (__any_sync(0xffffffffu, open)) {
+            k = k + 1;
+            continue;
+        }
+        if (valid && r.body != me && r.mass != 0) {
+            const double inv = nb_rsqrt_f64(d2 + eps2);
+            const double s = r.mass * inv * inv * inv;
+            acx = fma(s, dx, acx);
+            acy = fma(s, dy, acy);
+            acz = fma(s, dz, acz);
+        }
+        k = r.skip;
+    }
+    if (valid) {
+        ax[me] = acx * G;
+        ay[me] = acy * G;
+        az[me] = acz * G;
+    }
+}
+
+// Group rule, FP32 pair math; tile sums of 32 accepted cells folded into (hi, lo) by TwoSum.
+__global__ void __launch_bounds__(TR_THREADS)
+bh_group_f32_kernel(const NodeRec32* __restrict__ rec, const uint32_t* __restrict__ info,
+                    const uint32_t* __restrict__ ids, const double* __restrict__ x,
+                    const double* __restrict__ y, const double* __restrict__ z,
+                    const double* __restrict__ box, uint32_t n, float theta, float eps2,
+                    double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az) {
+    const uint32_t p = blockIdx.x * TR_THREADS + threadIdx.x;
+    const bool valid = p < n;
+    const uint32_t nn = info[0];
+    const uint32_t me = valid ? ids[p] : NB_NONE;
+    const double ox = box[0] + box[6] / 2, oy = box[1] + box[6] / 2, oz = box[2] + box[6] / 2;
+    float px = 0, py = 0, pz = 0;
+    if (valid) {
+        px = (float)(x[me] - ox);
+        py = (float)(y[me] - oy);
+        pz = (float)(z[me] - oz);
+    }
+    const float theta2 = theta * theta;
+    float tx = 0, ty = 0, tz = 0, hx = 0, hy = 0, hz = 0, lx = 0, ly = 0, lz = 0;
+    int batch = 0;
+    uint32_t k = 0;
+    while (k < nn) {
+        const NodeRec32 r = rec[k];
+        const float dx = r.cx - px, dy = r.cy - py, dz = r.cz - pz;
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const bool open = valid && r.body == NB_NONE && r.edge2 >= theta2 * d2;
+        if (__any_sync(0xffffffffu, open)) {
+            k = k + 1;
+            continue;
+        }
+        if (valid && r.body != me) {
+            const float inv = nb_rsqrt_f32(d2 + eps2);
+            const float s = r.gm * inv * inv * inv;
+            tx = fmaf(dx, s, tx);
+            ty = fmaf(dy, s, ty);
+            tz = fmaf(dz, s, tz);
+        }
+        if (++batch == 32) {
+            batch = 0;
+            float sh = hx + tx, bp = sh - hx;
+            lx += (hx - (sh - bp)) + (tx - bp);
+            hx = sh;
+            sh = hy + ty;
+            bp = sh - hy;
+            ly += (hy - (sh - bp)) + (ty - bp);
+            hy = sh;
+            sh = hz + tz;
+            bp = sh - hz;
+            lz += (hz - (sh - bp)) + (tz - bp);
+            hz = sh;
+            tx = ty = tz = 0;
+        }
+        k = r.skip;
+    }
+    if (valid) {
+        ax[me] = ((double)hx + (double)lx) + (double)tx;
+        ay[me] = ((double)hy + (double)ly) + (double)ty;
+        az[me] = ((double)hz + (double)lz) + (double)tz;
+    }
+}
+
+// Work model: per body, the number of cells accepted (interactions) and opened under the
+// per-body rule (FP64 decisions); totals accumulated into out[0] (accepted), out[1] (opened).
+__global__ void __launch_bounds__(TR_THREADS)
+bh_count_kernel(const NodeRec64* __restrict__ rec, const uint32_t* __restrict__ info,
+                const uint32_t* __restrict__ ids, const double* __restrict__ x,
+                const double* __restrict__ y, const double* __restrict__ z, uint32_t n,
+                double theta, int group, unsigned long long* __restrict__ out) {
+    const uint32_t p = blockIdx.x * TR_THREADS + threadIdx.x;
+    const bool valid = p < n;
+    const uint32_t nn = info[0];
+    const uint32_t me = valid ? ids[p] : NB_NONE;
+    double px = 0, py = 0, pz = 0;
+    if (valid) {
+        px = x[me];
+        py = y[me];
+        pz = z[me];
+    }
+    unsigned long long acc = 0, opened = 0;
+    uint32_t kl = valid ? 0u : nn;
+    const double theta2 = theta * theta;
+    for (;;) {
+        const uint32_t k = group ? (valid ? kl : nn) : kl;
+        const uint32_t kk = group ? __reduce_min_sync(0xffffffffu, k) : __reduce_min_sync(0xffffffffu, kl);
+        if (kk >= nn) break;
+        const NodeRec64 r = rec[kk];
+        const double dx = r.cx - px, dy = r.cy - py, dz = r.cz - pz;
+        const double d2 = fma(dx, dx, fma(dy, dy, dz * dz));
+        const bool wants_open = valid && r.mass != 0 && r.body == NB_NONE &&
+                                r.edge * r.edge >= theta2 * d2;
+        if (group) {
+            if (__any_sync(0xffffffffu, wants_open)) {
+                if (valid) opened += 1;
+                kl = kk + 1;
+            } else {
+                if (valid && r.body != me && r.mass != 0) acc += 1;
+                kl = r.skip;
+            }
+        } else if (kl == kk) {
+            if (r.mass == 0 || r.body == me) {
+                kl = r.skip;
+            } else if (wants_open) {
+                opened += 1;
+                kl = kk + 1;
+            } else {
+                acc += 1;
+                kl = r.skip;
+            }
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        acc += __shfl_down_sync(0xffffffffu, acc, off);
+        opened += __shfl_down_sync(0xffffffffu, opened, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&out[0], acc);
+        atomicAdd(&out[1], opened);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const double* y,
+                      const double* z, double* ax, double* ay, double* az, double G, double eps2,
+                      nb_opening opening, nb_precision prec, nb_stream_t stream_) {
+    NB_CHECK_CTX(ctx);
+    if (!t) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: null tree");
+    if (!t->built) return nb::set_error(NB_ERR_NOT_BUILT, "nb_bh_accel: tree not built");
+    if (!x || !y || !z || !ax || !ay || !az)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: null array");
+    cudaStream_t s = (cudaStream_t)stream_;
+    const uint32_t n = t->n;
+    const int grid = nb::ceil_div(n, TR_THREADS);
+    const double theta = t->params.theta;
+    if (opening == NB_OPEN_THETA) {
+        switch (prec) {
+            case NB_F64_IEEE:
+                bh_theta_f64_kernel<IEEE64><<<grid, TR_THREADS, 0, s>>>(
+                    t->rec64, t->info, t->ids, x, y, z, n, theta, eps2, G, ax, ay, az);
+                return nb::check_launch("bh_theta_f64_kernel<ieee>");
+            case NB_F64:
+                bh_theta_f64_kernel<FAST64><<<grid, TR_THREADS, 0, s>>>(
+                    t->rec64, t->info, t->ids, x, y, z, n, theta, eps2, G, ax, ay, az);
+                return nb::check_launch("bh_theta_f64_kernel");
+            case NB_F32C:
+                if (G != t->G)
+                    return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: G differs from the build's");
+                bh_theta_f32_kernel<<<grid, TR_THREADS, 0, s>>>(t->rec32, t->info, t->ids, x, y, z,
+                                                                t->box, n, (float)theta,
+                                                                (float)eps2, ax, ay, az);
+                return nb::check_launch("bh_theta_f32_kernel");
+            default:
+                break;
+        }
+    } else if (opening == NB_OPEN_THETA_GROUP) {
+        switch (prec) {
+            case NB_F64_IEEE:
+            case NB_F64:
+                bh_group_f64_kernel<<<grid, TR_THREADS, 0, s>>>(t->rec64, t->info, t->ids, x, y, z,
+                                                                n, theta, eps2, G, ax, ay, az);
+                return nb::check_launch("bh_group_f64_kernel");
+            case NB_F32C:
+                if (G != t->G)
+                    return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: G differs from the build's");
+                bh_group_f32_kernel<<<grid, TR_THREADS, 0, s>>>(t->rec32, t->info, t->ids, x, y, z,
+                                                                t->box, n, (float)theta,
+                                                                (float)eps2, ax, ay, az);
+                return nb::check_launch("bh_group_f32_kernel");
+            default:
+                break;
+        }
+    } else if (opening == NB_OPEN_LEARNED) {
+        return nb::set_error(NB_ERR_UNSUPPORTED, "nb_bh_accel: NB_OPEN_LEARNED needs a policy");
+    }
+    return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: unknown opening %d / precision %d",
+                         (int)opening, (int)prec);
+}
+
+nb_status nb_bh_count_interactions(nb_ctx* ctx, const nb_bh_tree* t, const double* x,
+                                   const double* y, const double* z, nb_opening opening,
+                                   unsigned long long* out_dev, nb_stream_t stream_) {
+    NB_CHECK_CTX(ctx);
+    if (!t || !t->built) return nb::set_error(NB_ERR_NOT_BUILT, "nb_bh_count_interactions: tree not built");
+    if (!x || !y || !z || !out_dev) return nb::set_error(NB_ERR_INVALID_ARG, "null pointer");
+    if (opening != NB_OPEN_THETA && opening != NB_OPEN_THETA_GROUP)
+        return nb::set_error(NB_ERR_UNSUPPORTED, "nb_bh_count_interactions: theta rules only");
+    cudaStream_t s = (cudaStream_t)stream_;
+    NB_CUDA_TRY(cudaMemsetAsync(out_dev, 0, 2 * sizeof(unsigned long long), s));
+    bh_count_kernel<<<nb::ceil_div(t->n, TR_THREADS), TR_THREADS, 0, s>>>(
+        t->rec64, t->info, t->ids, x, y, z, t->n, t->params.theta,
+        opening == NB_OPEN_THETA_GROUP ? 1 : 0, out_dev);
+    return nb::check_launch("bh_count_kernel");
+}
+
+}  // extern "C"

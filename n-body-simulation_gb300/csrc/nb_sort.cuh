@@ -1,0 +1,20 @@
+// nb_sort.cuh -- device-wide scan and radix sort used by the octree build.
+#pragma once
+#include "nb_internal.cuh"
+
+namespace nb {
+
+// Bytes of temporary storage exclusive_scan_u32 needs for n elements.
+size_t scan_temp_bytes(uint32_t n);
+// out[i] = sum(in[0..i)); with write_total, out[n] = sum(in[0..n)). In-place allowed.
+nb_status exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int write_total,
+                             uint32_t* temp, cudaStream_t stream);
+
+size_t radix_temp_bytes(uint32_t n);
+// Stable LSD sort of (keys, vals) on bits [begin_bit, end_bit) in 8-bit digits, ping-ponging
+// with (keys_alt, vals_alt); *result_in_alt says which pair holds the result.
+nb_status radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
+                           uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit,
+                           void* temp, cudaStream_t stream, int* result_in_alt);
+
+}  // namespace nb

@@ -152,3 +152,151 @@ class Context:
     def aabb(self, x, y, z, out, stream=None):
         check(self.lib.nb_aabb(self.handle, ptr(x), ptr(y), ptr(z), x.numel(), ptr(out),
                                stream_ptr(stream)))
+
+
+# -- Barnes-Hut ---------------------------------------------------------------------------------
+NB_OPEN_THETA, NB_OPEN_THETA_GROUP, NB_OPEN_LEARNED = 0, 1, 2
+OPENINGS = {"theta": NB_OPEN_THETA, "group": NB_OPEN_THETA_GROUP, "learned": NB_OPEN_LEARNED}
+
+
+class BHParams(C.Structure):
+    _fields_ = [("theta", C.c_double), ("storage_size_param", C.c_uint32),
+                ("stack_size_param", C.c_uint32), ("max_build_level", C.c_int),
+                ("sort_bodies", C.c_int)]
+
+
+class BHStats(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("node_count", C.c_uint32), ("max_depth", C.c_uint32),
+                ("ref_node_count", C.c_uint32), ("aabb", C.c_double * 7)]
+
+
+class BHRefLayout(C.Structure):
+    _fields_ = [("capacity", C.c_uint32), ("node_count", C.c_uint32),
+                ("octants", C.c_void_p), ("edge", C.c_void_p), ("min_x", C.c_void_p),
+                ("min_y", C.c_void_p), ("min_z", C.c_void_p), ("body_of_node", C.c_void_p),
+                ("node_is_leaf", C.c_void_p), ("sum_masses", C.c_void_p), ("com_x", C.c_void_p),
+                ("com_y", C.c_void_p), ("com_z", C.c_void_p), ("body_count", C.c_void_p),
+                ("sorted_bodies", C.c_void_p)]
+
+
+SIGNATURES.update({
+    "nb_bh_params_default": [C.POINTER(BHParams)],
+    "nb_bh_tree_create": [_vp, _u32, C.POINTER(BHParams), C.POINTER(_vp)],
+    "nb_bh_tree_destroy": [_vp],
+    "nb_bh_tree_set_theta": [_vp, _d],
+    "nb_bh_build": [_vp, _vp] + [_vp] * 4 + [_u32, _d, _vp],
+    "nb_bh_accel": [_vp, _vp] + [_vp] * 6 + [_d, _d, _i, _i, _vp],
+    "nb_bh_tree_stats": [_vp, C.POINTER(BHStats)],
+    "nb_bh_export_ref_layout": [_vp, C.POINTER(BHRefLayout)],
+    "nb_bh_export_order": [_vp, _vp, _vp],
+    "nb_util_radix_sort_pairs": [_vp, _vp, _vp, _u32, _i, _i, _vp],
+    "nb_util_exclusive_scan_u32": [_vp, _vp, _vp, _u32, _vp],
+    "nb_bh_count_interactions": [_vp, _vp, _vp, _vp, _vp, _i, _vp, _vp],
+    "nb_util_fma_peak": [_vp, _i, C.POINTER(_d)],
+})
+
+
+def default_bh_params(**kw) -> BHParams:
+    p = BHParams()
+    check(load().nb_bh_params_default(C.byref(p)))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class BHTree:
+    """Owns an nb_bh_tree (device memory for up to n_max bodies)."""
+
+    def __init__(self, ctx: Context, n_max: int, **params):
+        self.ctx = ctx
+        self.lib = load()
+        self.params = default_bh_params(**params)
+        h = _vp()
+        check(self.lib.nb_bh_tree_create(ctx.handle, n_max, C.byref(self.params), C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.nb_bh_tree_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_theta(self, theta):
+        check(self.lib.nb_bh_tree_set_theta(self.handle, theta))
+
+    def build(self, m, x, y, z, G, stream=None):
+        check(self.lib.nb_bh_build(self.ctx.handle, self.handle, ptr(m), ptr(x), ptr(y), ptr(z),
+                                   m.numel(), G, stream_ptr(stream)))
+
+    def accel(self, x, y, z, ax, ay, az, G, eps2, opening="theta", precision="f64", stream=None):
+        check(self.lib.nb_bh_accel(self.ctx.handle, self.handle, ptr(x), ptr(y), ptr(z), ptr(ax),
+                                   ptr(ay), ptr(az), G, eps2, OPENINGS[opening],
+                                   PRECISIONS[precision], stream_ptr(stream)))
+
+    def stats(self) -> dict:
+        s = BHStats()
+        check(self.lib.nb_bh_tree_stats(self.handle, C.byref(s)))
+        return {"n": s.n, "node_count": s.node_count, "max_depth": s.max_depth,
+                "ref_node_count": s.ref_node_count, "aabb": list(s.aabb)}
+
+    def count_interactions(self, x, y, z, opening="theta", stream=None):
+        """(accepted, opened) cell totals of a traversal under a theta rule."""
+        import torch
+        out = torch.zeros(2, dtype=torch.int64, device="cuda")
+        check(self.lib.nb_bh_count_interactions(self.ctx.handle, self.handle, ptr(x), ptr(y),
+                                                ptr(z), OPENINGS[opening], ptr(out),
+                                                stream_ptr(stream)))
+        self.ctx.sync(stream)
+        a, o = out.cpu().tolist()
+        return int(a), int(o)
+
+    def export_order(self, n):
+        import numpy as np
+        ids = np.zeros(n, dtype=np.uint32)
+        lvl = np.zeros(n, dtype=np.uint32)
+        check(self.lib.nb_bh_export_order(self.handle, ids.ctypes.data, lvl.ctypes.data))
+        return ids, lvl
+
+    def export_ref_layout(self, n):
+        """The reference's linearised octree arrays (numpy), trimmed to node_count."""
+        import numpy as np
+        st = self.stats()
+        cap = st["ref_node_count"]
+        arrs = {"octants": np.zeros(8 * cap, np.uint32), "edge": np.zeros(cap), "min_x": np.zeros(cap),
+                "min_y": np.zeros(cap), "min_z": np.zeros(cap),
+                "body_of_node": np.zeros(cap, np.uint32), "node_is_leaf": np.zeros(cap, np.int32),
+                "sum_masses": np.zeros(cap), "com_x": np.zeros(cap), "com_y": np.zeros(cap),
+                "com_z": np.zeros(cap), "body_count": np.zeros(cap, np.uint32),
+                "sorted_bodies": np.zeros(max(n, 1), np.uint32)}
+        lay = BHRefLayout()
+        lay.capacity = cap
+        for k, a in arrs.items():
+            setattr(lay, k, a.ctypes.data)
+        check(self.lib.nb_bh_export_ref_layout(self.handle, C.byref(lay)))
+        nc = lay.node_count
+        out = {k: (v[:nc] if k not in ("octants", "sorted_bodies") else v) for k, v in arrs.items()}
+        out["octants"] = arrs["octants"].reshape(8, cap)[:, :nc]
+        out["sorted_bodies"] = arrs["sorted_bodies"][:n]
+        out["node_count"] = nc
+        return out
+
+
+def fma_peak(ctx: Context, fp64: bool) -> float:
+    v = C.c_double(0)
+    check(load().nb_util_fma_peak(ctx.handle, 1 if fp64 else 0, C.byref(v)))
+    return v.value
+
+
+def util_radix_sort_pairs(ctx: Context, keys, vals, begin_bit=0, end_bit=64, stream=None):
+    check(load().nb_util_radix_sort_pairs(ctx.handle, ptr(keys), ptr(vals), keys.numel(),
+                                          begin_bit, end_bit, stream_ptr(stream)))
+
+
+def util_exclusive_scan_u32(ctx: Context, inp, out, stream=None):
+    check(load().nb_util_exclusive_scan_u32(ctx.handle, ptr(inp), ptr(out), inp.numel(),
+                                            stream_ptr(stream)))

@@ -77,6 +77,8 @@ def lib():
         L.orc_sort_bodies_for_subtrees.argtypes = [_up, C.c_uint32, _up, _up, C.c_uint32, _up, _up]
         L.orc_bh_accel.argtypes = [C.c_void_p] + [_dp] * 6 + [C.c_double] * 3 + [C.c_uint32, C.c_int,
                                                                                  C.c_int]
+        L.orc_bh_accel_subset.argtypes = [C.c_void_p] + [_dp] * 3 + [_up, C.c_uint32] + [_dp] * 3 + [
+            C.c_double] * 3 + [C.c_uint32, C.c_int]
         L.orc_bh_interaction_counts.argtypes = [C.c_void_p] + [_dp] * 3 + [C.c_double, C.c_uint32,
                                                                            _u64p, _u64p, C.c_int]
         L.orc_stack_size.restype = C.c_uint32
@@ -268,6 +270,20 @@ def bh_accel(tree: OracleTree, x, y, z, G, eps2, theta, stack_size_words=None, s
     ax, ay, az = (np.zeros(n) for _ in range(3))
     _check(lib().orc_bh_accel(tree.handle.ptr, _d(x), _d(y), _d(z), _d(ax), _d(ay), _d(az), G, eps2,
                               theta, stack_size_words, int(sorted_order), threads), "bh_accel")
+    return ax, ay, az
+
+
+def bh_accel_subset(tree: OracleTree, x, y, z, targets, G, eps2, theta, stack_size_words=None,
+                    threads=0):
+    x, y, z = map(_f64, (x, y, z))
+    targets = np.ascontiguousarray(targets, dtype=np.uint32)
+    if stack_size_words is None:
+        stack_size_words = stack_size(tree.n)
+    k = len(targets)
+    ax, ay, az = (np.zeros(k) for _ in range(3))
+    _check(lib().orc_bh_accel_subset(tree.handle.ptr, _d(x), _d(y), _d(z), _u(targets), k, _d(ax),
+                                     _d(ay), _d(az), G, eps2, theta, stack_size_words, threads),
+           "bh_accel_subset")
     return ax, ay, az
 
 

@@ -688,6 +688,60 @@ int orc_bh_accel(const orc_tree* t, const double* x, const double* y, const doub
     return err.load();
 }
 
+// Same traversal for a subset of target bodies (bounded CPU samples at large N); results are
+// written to ax[t] for targets[t].
+int orc_bh_accel_subset(const orc_tree* t, const double* x, const double* y, const double* z,
+                        const uint32_t* targets, uint32_t n_targets, double* ax, double* ay,
+                        double* az, double G, double eps2, double theta, uint32_t stack_size,
+                        int threads) {
+    if (!t || stack_size < 2 || !targets) return ORC_ERR_INVALID_ARG;
+    const uint32_t N = t->n;
+    const size_t S = t->S;
+    const int T = resolve_threads(threads);
+    std::atomic<int> err(ORC_OK);
+#pragma omp parallel num_threads(T)
+    {
+        std::vector<uint32_t> stack(stack_size);
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t q = 0; q < (int64_t)n_targets; ++q) {
+            const uint32_t i = targets[q];
+            const double px = x[i], py = y[i], pz = z[i];
+            double acc_x = 0, acc_y = 0, acc_z = 0;
+            uint32_t top = 1;
+            stack[top] = 0;
+            while (top != 0) {
+                const uint32_t node = stack[top--];
+                const double sm = t->sum_masses[node];
+                if (sm != 0 && t->body_of_node[node] != i) {
+                    double d_x = (t->com_x[node] / sm) - px;
+                    double d_y = (t->com_y[node] / sm) - py;
+                    double d_z = (t->com_z[node] / sm) - pz;
+                    double d = rsqrt_ref(d_x * d_x + d_y * d_y + d_z * d_z);
+                    if ((t->edge[node] * d < theta) || t->body_of_node[node] != N) {
+                        double den = (d_x * d_x) + (d_y * d_y) + (d_z * d_z) + eps2;
+                        den = den * den * den;
+                        den = rsqrt_ref(den);
+                        acc_x += sm * (d_x * den);
+                        acc_y += sm * (d_y * den);
+                        acc_z += sm * (d_z * den);
+                    } else {
+                        if (top + 8 > stack_size - 1) {
+                            err.store(ORC_ERR_STACK_OVERFLOW);
+                            break;
+                        }
+                        static const uint32_t push_order[8] = {5, 7, 4, 6, 1, 3, 0, 2};
+                        for (int k = 0; k < 8; ++k) stack[++top] = t->octants[push_order[k] * S + node];
+                    }
+                }
+            }
+            ax[q] = acc_x * G;
+            ay[q] = acc_y * G;
+            az[q] = acc_z * G;
+        }
+    }
+    return err.load();
+}
+
 // Per-body count of accepted nodes and opened nodes for the reference traversal (work model).
 int orc_bh_interaction_counts(const orc_tree* t, const double* x, const double* y,
                               const double* z, double theta, uint32_t stack_size,

@@ -1,0 +1,204 @@
+"""Parity of the Barnes-Hut path against the CPU oracle restating the reference
+(ParallelOctreeTopDownSubtrees.cpp, BarnesHutOctree.cpp, BarnesHutAlgorithm.cpp:280-401),
+through the C ABI.
+
+* radix sort / scan building blocks: exact vs numpy.
+* tree: the reference's known answers, and cell-by-cell equality (octants, cell corners, edge,
+  FP64 mass and centre-of-mass sums, body counts, in-order body sort) with the oracle's tree.
+* accelerations, reference rule: NB_F64_IEEE bit-identical to the oracle's traversal; NB_F64
+  within 1e-12 relative per body.
+* group rule / FP32: within stated bounds of the naive FP64 oracle.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import bodies, canonical_compare, dev, host, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from nbody.lib import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def build(ctx, d, **params):
+    from nbody.lib import BHTree
+    t = BHTree(ctx, len(d["m"]), **params)
+    dd = {k: dev(d[k]) for k in ("m", "x", "y", "z")}
+    t.build(dd["m"], dd["x"], dd["y"], dd["z"], d["G"])
+    ctx.sync()
+    return t, dd
+
+
+def accel(ctx, t, dd, G, eps2, opening, precision):
+    import torch
+    n = dd["x"].numel()
+    a = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    t.accel(dd["x"], dd["y"], dd["z"], *a, G, eps2, opening, precision)
+    ctx.sync()
+    return [host(v) for v in a]
+
+
+# -- building blocks ----------------------------------------------------------------------------
+@pytest.mark.parametrize("n", [1, 2, 2047, 2048, 2049, 100000])
+def test_radix_sort_stable(ctx, n):
+    import torch
+    from nbody.lib import util_radix_sort_pairs
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 1 << 20, size=n, dtype=np.uint64) << np.uint64(40)
+    keys |= rng.integers(0, 4, size=n, dtype=np.uint64)  # many duplicates
+    vals = np.arange(n, dtype=np.uint32)
+    tk = torch.as_tensor(keys.view(np.int64), device="cuda")
+    tv = torch.as_tensor(vals.view(np.int32), device="cuda")
+    util_radix_sort_pairs(ctx, tk, tv, 0, 63)
+    ctx.sync()
+    order = np.argsort(keys, kind="stable")
+    np.testing.assert_array_equal(tk.cpu().numpy().view(np.uint64), keys[order])
+    np.testing.assert_array_equal(tv.cpu().numpy().view(np.uint32), vals[order])
+
+
+@pytest.mark.parametrize("n", [1, 1023, 4096, 4097, 1 << 20])
+def test_exclusive_scan(ctx, n):
+    import torch
+    from nbody.lib import util_exclusive_scan_u32
+    rng = np.random.default_rng(n)
+    a = rng.integers(0, 9, size=n, dtype=np.uint32)
+    tin = torch.as_tensor(a.view(np.int32), device="cuda")
+    tout = torch.zeros(n + 1, dtype=torch.int32, device="cuda")
+    util_exclusive_scan_u32(ctx, tin, tout)
+    ctx.sync()
+    ref = np.concatenate([[0], np.cumsum(a, dtype=np.uint64)]).astype(np.uint32)
+    np.testing.assert_array_equal(tout.cpu().numpy().view(np.uint32), ref)
+
+
+# -- tree ---------------------------------------------------------------------------------------
+def test_reference_known_answers(ctx, kats):
+    t = [t for t in kats["BarnesHutTest.cpp"] if t["name"] == "buildOctreeSubtreesTest"][0]
+    v = t["vectors"]
+    d = {"m": np.array(v["masses"], float), "x": np.array(v["x_positions"], float),
+         "y": np.array(v["y_positions"], float), "z": np.array(v["z_positions"], float), "G": 1.0}
+    tree, _ = build(ctx, d, max_build_level=1)
+    lay = tree.export_ref_layout(3)
+    assert lay["node_count"] == 9
+    for e in t["expects"]:
+        arr = {"BODY_OF_NODE": "body_of_node", "SUM_MASSES": "sum_masses",
+               "SORTED_BODIES": "sorted_bodies"}[e["array"]]
+        assert lay[arr][e["index"]] == pytest.approx(e["value"]), e
+
+
+def _clustered(n, seed):
+    """Tight clumps with near-coincident pairs: forces leaves below 21 levels (second key word)."""
+    rng = np.random.default_rng(seed)
+    c = rng.normal(size=(3, n // 4))
+    pts = np.repeat(c, 4, axis=1)
+    pts[:, 1::4] += 1e-8 * rng.normal(size=(3, n // 4))
+    pts[:, 2::4] += 1e-5 * rng.normal(size=(3, n // 4))
+    pts[:, 3::4] += 1e-10 * rng.normal(size=(3, n // 4))
+    return {"m": rng.uniform(1, 2, n // 4 * 4), "x": pts[0].copy(), "y": pts[1].copy(),
+            "z": pts[2].copy(), "G": 1.0}
+
+
+@pytest.mark.parametrize("case", ["disc-2000", "plummer-5000", "disc-1", "disc-2", "plummer-3",
+                                  "clustered-4000", "shifted-3000"])
+def test_tree_matches_oracle_cell_by_cell(ctx, case):
+    kind, n = case.split("-")
+    n = int(n)
+    if kind == "clustered":
+        d = _clustered(n, 3)
+    elif kind == "shifted":
+        d = bodies("plummer", n, seed=9)
+        d["x"] = d["x"] + 25.0  # box must still contain the origin (reference convention)
+    else:
+        d = bodies(kind, n, seed=5)
+    # deep clumps need more than the reference's default 16*N node slots (each level of a
+    # single-child chain costs 8 slots there)
+    storage = 256 if kind == "clustered" else 16
+    ot = oracle.build_subtrees(d["m"], d["x"], d["y"], d["z"], max_level=7, threads=4,
+                               storage_param=storage)
+    tree, _ = build(ctx, d)
+    st = tree.stats()
+    assert st["ref_node_count"] == ot.node_count
+    assert st["node_count"] <= 2 * len(d["m"]) - 1
+    np.testing.assert_array_equal(np.array(st["aabb"]), ot.aabb)
+    lay = tree.export_ref_layout(len(d["m"]))
+    cells = canonical_compare(ot, lay, len(d["m"]))
+    assert cells == ot.node_count
+    if kind == "clustered":
+        assert st["max_depth"] > 21  # exercised the second key word
+
+
+def test_coincident_bodies_report_depth_overflow(ctx):
+    from nbody.lib import NBodyError, BHTree
+    d = bodies("plummer", 100, seed=1)
+    d["x"][7], d["y"][7], d["z"][7] = d["x"][3], d["y"][3], d["z"][3]
+    t = BHTree(ctx, 100)
+    dd = {k: dev(d[k]) for k in ("m", "x", "y", "z")}
+    t.build(dd["m"], dd["x"], dd["y"], dd["z"], 1.0)
+    with pytest.raises(NBodyError, match="DEPTH"):
+        ctx.sync()
+    ctx.sync()  # error word cleared; context still usable
+    d2 = bodies("plummer", 100, seed=2)
+    t.build(*[dev(d2[k]) for k in ("m", "x", "y", "z")], 1.0)
+    ctx.sync()
+
+
+# -- accelerations ------------------------------------------------------------------------------
+@pytest.mark.parametrize("kind,n,theta", [("disc", 3000, 0.5), ("disc", 3000, 1.05),
+                                          ("plummer", 4000, 0.5), ("plummer", 2, 0.5),
+                                          ("plummer", 1, 0.5), ("clustered", 2000, 0.7),
+                                          ("plummer", 1500, 0.0)])
+def test_accel_theta_ieee_bit_identical(ctx, kind, n, theta):
+    d = _clustered(n, 4) if kind == "clustered" else bodies(kind, n, seed=8)
+    eps2 = 1e-22 if kind == "disc" else 1e-6
+    ot = oracle.build_subtrees(d["m"], d["x"], d["y"], d["z"], threads=4,
+                               storage_param=256 if kind == "clustered" else 16)
+    ref = oracle.bh_accel(ot, d["x"], d["y"], d["z"], d["G"], eps2, theta, threads=4)
+    tree, dd = build(ctx, d, theta=theta)
+    got = accel(ctx, tree, dd, d["G"], eps2, "theta", "f64_ieee")
+    for g, r in zip(got, ref):
+        np.testing.assert_array_equal(g, r)
+    fast = accel(ctx, tree, dd, d["G"], eps2, "theta", "f64")
+    if n > 1:
+        assert rel_err(*fast, *ref).max() <= 1e-12
+
+
+def test_theta_zero_equals_direct_sum(ctx):
+    d = bodies("plummer", 700, seed=12)
+    tree, dd = build(ctx, d, theta=0.0)
+    got = accel(ctx, tree, dd, 1.0, 1e-6, "theta", "f64")
+    ref = oracle.naive_accel(d["m"], d["x"], d["y"], d["z"], 1.0, 1e-6)
+    assert rel_err(*got, *ref).max() <= 1e-12
+
+
+@pytest.mark.parametrize("kind,n", [("disc", 20000), ("plummer", 20000)])
+def test_group_rule_and_f32(ctx, kind, n):
+    d = bodies(kind, n, seed=21)
+    eps2 = 1e-22 if kind == "disc" else 1e-6
+    naive = oracle.naive_accel(d["m"], d["x"], d["y"], d["z"], d["G"], eps2)
+    tree, dd = build(ctx, d, theta=0.5)
+    e_theta = rel_err(*accel(ctx, tree, dd, d["G"], eps2, "theta", "f64"), *naive)
+    e_group = rel_err(*accel(ctx, tree, dd, d["G"], eps2, "group", "f64"), *naive)
+    e_group32 = rel_err(*accel(ctx, tree, dd, d["G"], eps2, "group", "f32c"), *naive)
+    e_theta32 = rel_err(*accel(ctx, tree, dd, d["G"], eps2, "theta", "f32c"), *naive)
+    # the group rule opens a superset of cells: never less accurate in the median
+    assert np.median(e_group) <= np.median(e_theta) * 1.0001
+    assert np.median(e_theta) <= 5e-3
+    # FP32 pair math adds ~1e-6 on top of the approximation error
+    assert abs(np.median(e_group32) - np.median(e_group)) <= 1e-5 + 0.05 * np.median(e_group)
+    assert abs(np.median(e_theta32) - np.median(e_theta)) <= 1e-5 + 0.05 * np.median(e_theta)
+    assert np.all(np.isfinite(e_group32))
+
+
+def test_accel_before_build_is_rejected(ctx):
+    import torch
+    from nbody.lib import BHTree, NBodyError
+    t = BHTree(ctx, 10)
+    z = torch.zeros(10, dtype=torch.float64, device="cuda")
+    with pytest.raises(NBodyError, match="NOT_BUILT"):
+        t.accel(z, z, z, z, z, z, 1.0, 0.0)
