@@ -115,6 +115,20 @@ nb_status nb_energy(nb_ctx* ctx, const double* m, const double* x, const double*
                     const double* z, const double* vx, const double* vy, const double* vz,
                     uint32_t n, double G, double* out_dev, nb_stream_t stream);
 
+/* Energy for callers that cannot let the library allocate device memory (no counterpart in the
+ * reference). Same result as nb_energy, but needs no context and never calls cudaMalloc,
+ * cudaFree or any allocating routine: the per-block partial sums live in a fixed 128 KiB
+ * file-scope device array, present on every GPU that loads the library until the process exits.
+ * Limit: n <= NB_ENERGY_NOALLOC_MAX_N bodies (larger n returns NB_ERR_INVALID_ARG).
+ * Runs on the current device. Its first call on each device looks up that array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream capture. All calls
+ * share the array: calls that overlap on the GPU race, so serialise them (one stream at a
+ * time). out_dev: DEVICE pointer to 4 doubles {kinetic, potential, total, virial}. */
+#define NB_ENERGY_NOALLOC_MAX_N 1048576u
+nb_status nb_energy_noalloc(const double* m, const double* x, const double* y, const double* z,
+                            const double* vx, const double* vy, const double* vz, uint32_t n,
+                            double G, double* out_dev, nb_stream_t stream);
+
 /* ---------------------------------------------------------------------------------------------
  * AABB. Replaces BarnesHutOctree::computeMinMaxValuesAABB (BarnesHutOctree.cpp:45-191),
  * including its conventions: the box always contains the origin (the reference's partial

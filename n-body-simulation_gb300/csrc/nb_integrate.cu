@@ -1,4 +1,6 @@
 // nb_integrate.cu -- leapfrog kick-drift-kick, energy and AABB kernels (all FP64).
+#include <mutex>
+
 #include "nb_internal.cuh"
 
 namespace {
@@ -355,6 +357,75 @@ nb_status nb_aabb(nb_ctx* ctx, const double* x, const double* y, const double* z
     NB_CHECK_CTX(ctx);
     if (!x || !y || !z || !out_dev) return nb::set_error(NB_ERR_INVALID_ARG, "nb_aabb: null pointer");
     return nb::launch_aabb(ctx, x, y, z, n, out_dev, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Energy without any allocation.
+//
+// Some callers cannot let this library allocate device memory: an application that reserves the
+// GPU's memory up front for its own pool and forbids later cudaMalloc calls, or a time-critical
+// loop that cannot pay for cudaMalloc's device-wide synchronisation and unpredictable latency.
+// nb_energy needs a context (whose creation allocates) and grows per-block scratch on demand;
+// nb_energy_noalloc runs the same two kernels with their per-block partial sums in the fixed
+// array below instead. Nothing in the array needs clearing between calls: every call writes each
+// partial it later reads. All calls share the array, so calls that overlap on the GPU (two
+// streams, two host threads) race and must be serialised by the caller.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_BLOCKS = 8192;  // 8192 * 16 B = 128 KiB of scratch per device
+static_assert(NB_ENERGY_NOALLOC_MAX_N == NOALLOC_MAX_BLOCKS * EN_THREADS, "size mismatch");
+
+// Per-block (kinetic, potential) partials. Every GPU that loads the library holds this array
+// until the process exits. Host code must not pass the symbol itself to a kernel: its host-side
+// name is only a stand-in, so the device address is looked up once per device below.
+static __device__ __align__(256) double2 g_energy_noalloc_partials[NOALLOC_MAX_BLOCKS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the partials array on the current device (looked up on first use).
+nb_status noalloc_partials(double2** out) {
+    int dev = -1;
+    NB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return nb::set_error(NB_ERR_UNSUPPORTED, "nb_energy_noalloc: device %d not supported", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_energy_noalloc_partials);
+        if (e != cudaSuccess) return nb::cuda_error(e, "nb_energy_noalloc: cudaGetSymbolAddress");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = (double2*)g_noalloc_addr[dev];
+    return NB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+nb_status nb_energy_noalloc(const double* m, const double* x, const double* y, const double* z,
+                            const double* vx, const double* vy, const double* vz, uint32_t n,
+                            double G, double* out_dev, nb_stream_t stream) {
+    if (!m || !x || !y || !z || !vx || !vy || !vz || !out_dev)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_energy_noalloc: null pointer");
+    if (n == 0) return nb::set_error(NB_ERR_INVALID_ARG, "nb_energy_noalloc: n == 0");
+    if (n > NB_ENERGY_NOALLOC_MAX_N)
+        return nb::set_error(NB_ERR_INVALID_ARG,
+                             "nb_energy_noalloc: n = %u exceeds the fixed scratch limit of %u "
+                             "bodies; use nb_energy", n, (unsigned)NB_ENERGY_NOALLOC_MAX_N);
+    double2* part = nullptr;
+    NB_TRY(noalloc_partials(&part));
+    const uint32_t blocks = (n + EN_THREADS - 1) / EN_THREADS;
+    energy_kernel<<<blocks, EN_THREADS, 0, (cudaStream_t)stream>>>(m, x, y, z, vx, vy, vz, n, G,
+                                                                  part);
+    NB_TRY(nb::check_launch("energy_kernel (noalloc)"));
+    energy_finalize<<<1, 256, 0, (cudaStream_t)stream>>>(part, blocks, out_dev);
+    return nb::check_launch("energy_finalize (noalloc)");
 }
 
 }  // extern "C"

@@ -45,6 +45,7 @@ SIGNATURES = {
     "nb_leapfrog_kick_kick_drift": [_vp] + [_vp] * 12 + [_u32, _d, _vp],
     "nb_energy": [_vp] + [_vp] * 7 + [_u32, _d, _vp, _vp],
     "nb_aabb": [_vp] + [_vp] * 3 + [_u32, _vp, _vp],
+    "nb_energy_noalloc": [_vp] * 7 + [_u32, _d, _vp, _vp],
 }
 STRING_FUNCS = ("nb_last_error_string", "nb_version")
 
