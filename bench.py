@@ -426,6 +426,7 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
 
 
 def main():
+    global N_BODIES
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -433,9 +434,12 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the secondary measurements")
+    ap.add_argument("--bodies", type=int, default=N_BODIES,
+                    help="bodies of the disc (default 1,048,576; smaller only for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    N_BODIES = args.bodies
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
