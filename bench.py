@@ -43,6 +43,7 @@ LAUNCHES_PER_STEP = 53
 # algorithmic FLOP of the traversal (Nyland's 20 per pair interaction for an accepted cell; an
 # opened cell costs its distance test: 3 sub, 3 mul, 2 add, 1 rsqrt, 1 mul = 10)
 FLOP_ACCEPTED, FLOP_OPENED = 20, 10
+TRAVERSAL_KERNEL = "bh_theta_lane_kernel"
 
 
 def dist_env():
@@ -106,12 +107,14 @@ class ClockSampler:
 
 
 def load_traffic(name):
+    """(bytes per launch, source) of a kernel from the committed ncu summary, or (None, None)."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(name)
-    except (OSError, ValueError):
-        return None
+            e = json.load(f).get(name)
+        return (e["bytes_per_launch"], e["source"]) if e else (None, None)
+    except (OSError, ValueError, KeyError):
+        return None, None
 
 
 def measured_hbm_peak():
@@ -352,10 +355,11 @@ def run_ours(args):
                     "h2d_bytes_per_step": 8 * n * len(h2d_arrays),
                     "d2h_bytes_per_step": 8 * n * 9},
             "gpu_launches": LAUNCHES_PER_STEP * args.steps,
-            "roofline": {"kernel": "bh_theta_f64_kernel (traversal)", "bound": "fp64",
+            "roofline": {"kernel": TRAVERSAL_KERNEL + " (traversal)", "bound": "fp64",
                          "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
                          "unit": "TFLOP/s", "frac": achieved / fp64_peak,
-                         "traffic": load_traffic("bh_theta_f64_kernel"),
+                         "traffic": load_traffic(TRAVERSAL_KERNEL)[0],
+                         "traffic_source": load_traffic(TRAVERSAL_KERNEL)[1],
                          "peak_source": "FP64 FMA throughput measured in this run "
                                         "(nb_util_fma_peak)",
                          "work": {"accepted_cells": accepted, "opened_cells": opened,
@@ -365,7 +369,7 @@ def run_ours(args):
                                "frac": build_bytes / (build_ms * 1e-3) / 1e9 / hbm_peak,
                                "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
                                "ms_per_build": build_ms, "algorithmic_bytes": build_bytes,
-                               "traffic": load_traffic("bh_build")},
+                               "traffic": load_traffic("bh_build")[0]},
             "tree": {"nodes": nodes, "max_depth": stats["max_depth"],
                      "reference_layout_nodes": stats["ref_node_count"]},
             "clocks": clk,

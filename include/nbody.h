@@ -220,6 +220,11 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* tree, const double* x, cons
                       const double* z, double* ax, double* ay, double* az, double G, double eps2,
                       nb_opening opening, nb_precision prec, nb_stream_t stream);
 
+/* Execution schedule of the per-body FP64 traversal (process-wide): 0 (default) = every lane
+ * walks its own body's DFS sequence with an FP32 pre-test of the opening rule; 1 = the warp walks
+ * the union of its 32 sequences in lockstep. Results are identical; this exists for comparison. */
+nb_status nb_bh_set_schedule(int lockstep);
+
 /* Synchronous. */
 nb_status nb_bh_tree_stats(nb_bh_tree* tree, nb_bh_stats* out);
 nb_status nb_bh_export_ref_layout(nb_bh_tree* tree, nb_bh_ref_layout* out);

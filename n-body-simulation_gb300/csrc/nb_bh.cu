@@ -256,9 +256,9 @@ __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double 
                               double sm, int level, uint32_t skip, uint32_t body) {
     const double edge = ldexp(A.box[6], -level);
     NodeRec64 r;
-    r.cx = __ddiv_rn(cx, sm);
-    r.cy = __ddiv_rn(cy, sm);
-    r.cz = __ddiv_rn(cz, sm);
+    r.cx = sm != 0 ? __ddiv_rn(cx, sm) : 0.0;  // massless cells: finite centre (never used)
+    r.cy = sm != 0 ? __ddiv_rn(cy, sm) : 0.0;
+    r.cz = sm != 0 ? __ddiv_rn(cz, sm) : 0.0;
     r.mass = sm;
     r.edge = edge;
     r.skip = skip;

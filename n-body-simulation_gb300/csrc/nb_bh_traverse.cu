@@ -103,6 +103,79 @@ bh_theta_f64_kernel(const NodeRec64* __restrict__ rec, const uint32_t* __restric
     }
 }
 
+// Per-body reference rule, FP64, each lane walking its own DFS sequence (no union walk).
+// The opening test is decided in FP32 on the anchored FP32 records whenever the FP32 error
+// bound proves the answer; only undecided cells evaluate the reference's FP64 expression.
+// FP32 error bound of d^2 with positions rounded relative to the box centre (|c-a|, |p-a| <=
+// E/2 per axis, u = 2^-24): |d2f - d2| <= u d^2 (2*sqrt(3) E/d + 5); the test below widens it
+// by 4x and adds the roundings of edge^2 and theta^2*d2f. Accumulation order per body is the
+// reference's DFS order, so MODE IEEE64 stays bit-identical.
+template <int MODE>
+__global__ void __launch_bounds__(TR_THREADS)
+bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __restrict__ rec64,
+                     const uint32_t* __restrict__ info, const uint32_t* __restrict__ ids,
+                     const double* __restrict__ x, const double* __restrict__ y,
+                     const double* __restrict__ z, const double* __restrict__ box, uint32_t n,
+                     double theta, double eps2, double G, double* __restrict__ ax,
+                     double* __restrict__ ay, double* __restrict__ az) {
+    using A = Arith<MODE>;
+    const uint32_t p = blockIdx.x * TR_THREADS + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t nn = info[0];
+    const uint32_t me = ids[p];
+    const double px = x[me], py = y[me], pz = z[me];
+    const double E = box[6];
+    const double ox = box[0] + E / 2, oy = box[1] + E / 2, oz = box[2] + E / 2;
+    const float pxf = (float)(px - ox), pyf = (float)(py - oy), pzf = (float)(pz - oz);
+    const float th2 = (float)(theta * theta);
+    const float u4 = 4.0f * 5.9604645e-8f;  // 4 * 2^-24
+    const float Ef = (float)E;
+    double acx = 0, acy = 0, acz = 0;
+    uint32_t k = 0;
+    while (k < nn) {
+        const NodeRec32 r = rec32[k];
+        if (r.body == me) {
+            k = r.skip;
+            continue;
+        }
+        bool accept = r.body != NB_NONE;
+        if (!accept) {
+            const float dxf = r.cx - pxf, dyf = r.cy - pyf, dzf = r.cz - pzf;
+            const float d2f = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
+            const float t = th2 * d2f;
+            const float rel = u4 * (3.5f * Ef * nb_rsqrt_f32(d2f) + 8.0f);
+            const float margin = t * rel + u4 * r.edge2;
+            if (r.edge2 > t + margin) {
+                accept = false;  // certainly opened
+            } else if (r.edge2 < t - margin) {
+                accept = true;   // certainly accepted
+            } else {             // undecided: the reference's FP64 expression
+                const NodeRec64 q = rec64[k];
+                const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py), dz = A::sub(q.cz, pz);
+                accept = A::mul(q.edge, A::rsqrt(A::norm2(dx, dy, dz))) < theta;
+            }
+        }
+        if (accept) {
+            const NodeRec64 q = rec64[k];
+            if (q.mass != 0) {
+                const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py), dz = A::sub(q.cz, pz);
+                double den = A::add(A::norm2(dx, dy, dz), eps2);
+                den = A::mul(A::mul(den, den), den);
+                const double inv = A::rsqrt(den);
+                acx = A::accum(acx, q.mass, dx, inv);
+                acy = A::accum(acy, q.mass, dy, inv);
+                acz = A::accum(acz, q.mass, dz, inv);
+            }
+            k = r.skip;
+        } else {
+            k = k + 1;
+        }
+    }
+    ax[me] = A::mul(acx, G);
+    ay[me] = A::mul(acy, G);
+    az[me] = A::mul(acz, G);
+}
+
 // Per-body reference rule with FP32 pair math and compensated accumulation.
 __global__ void __launch_bounds__(TR_THREADS)
 bh_theta_f32_kernel(const NodeRec32* __restrict__ rec, const uint32_t* __restrict__ info,
@@ -329,9 +402,18 @@ bh_count_kernel(const NodeRec64* __restrict__ rec, const uint32_t* __restrict__ 
     }
 }
 
+// Schedule of the per-body FP64 traversal: 0 = per-lane walks (default), 1 = the warp's union
+// walk (bh_theta_f64_kernel). Both produce identical results; the switch exists for comparison.
+int g_lockstep = 0;
+
 }  // namespace
 
 extern "C" {
+
+nb_status nb_bh_set_schedule(int lockstep) {
+    g_lockstep = lockstep ? 1 : 0;
+    return NB_OK;
+}
 
 nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const double* y,
                       const double* z, double* ax, double* ay, double* az, double G, double eps2,
@@ -348,13 +430,25 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
     if (opening == NB_OPEN_THETA) {
         switch (prec) {
             case NB_F64_IEEE:
-                bh_theta_f64_kernel<IEEE64><<<grid, TR_THREADS, 0, s>>>(
-                    t->rec64, t->info, t->ids, x, y, z, n, theta, eps2, G, ax, ay, az);
-                return nb::check_launch("bh_theta_f64_kernel<ieee>");
+                if (g_lockstep) {
+                    bh_theta_f64_kernel<IEEE64><<<grid, TR_THREADS, 0, s>>>(
+                        t->rec64, t->info, t->ids, x, y, z, n, theta, eps2, G, ax, ay, az);
+                    return nb::check_launch("bh_theta_f64_kernel<ieee>");
+                }
+                bh_theta_lane_kernel<IEEE64><<<grid, TR_THREADS, 0, s>>>(
+                    t->rec32, t->rec64, t->info, t->ids, x, y, z, t->box, n, theta, eps2, G, ax,
+                    ay, az);
+                return nb::check_launch("bh_theta_lane_kernel<ieee>");
             case NB_F64:
-                bh_theta_f64_kernel<FAST64><<<grid, TR_THREADS, 0, s>>>(
-                    t->rec64, t->info, t->ids, x, y, z, n, theta, eps2, G, ax, ay, az);
-                return nb::check_launch("bh_theta_f64_kernel");
+                if (g_lockstep) {
+                    bh_theta_f64_kernel<FAST64><<<grid, TR_THREADS, 0, s>>>(
+                        t->rec64, t->info, t->ids, x, y, z, n, theta, eps2, G, ax, ay, az);
+                    return nb::check_launch("bh_theta_f64_kernel");
+                }
+                bh_theta_lane_kernel<FAST64><<<grid, TR_THREADS, 0, s>>>(
+                    t->rec32, t->rec64, t->info, t->ids, x, y, z, t->box, n, theta, eps2, G, ax,
+                    ay, az);
+                return nb::check_launch("bh_theta_lane_kernel");
             case NB_F32C:
                 if (G != t->G)
                     return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: G differs from the build's");

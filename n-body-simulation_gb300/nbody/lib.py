@@ -194,6 +194,7 @@ SIGNATURES.update({
     "nb_util_exclusive_scan_u32": [_vp, _vp, _vp, _u32, _vp],
     "nb_bh_count_interactions": [_vp, _vp, _vp, _vp, _vp, _i, _vp, _vp],
     "nb_util_fma_peak": [_vp, _i, C.POINTER(_d)],
+    "nb_bh_set_schedule": [_i],
 })
 
 
@@ -285,6 +286,10 @@ class BHTree:
         out["sorted_bodies"] = arrs["sorted_bodies"][:n]
         out["node_count"] = nc
         return out
+
+
+def set_bh_schedule(lockstep: bool):
+    check(load().nb_bh_set_schedule(1 if lockstep else 0))
 
 
 def fma_peak(ctx: Context, fp64: bool) -> float:

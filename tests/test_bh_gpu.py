@@ -202,3 +202,18 @@ def test_accel_before_build_is_rejected(ctx):
     z = torch.zeros(10, dtype=torch.float64, device="cuda")
     with pytest.raises(NBodyError, match="NOT_BUILT"):
         t.accel(z, z, z, z, z, z, 1.0, 0.0)
+
+
+@pytest.mark.parametrize("precision", ["f64_ieee", "f64"])
+def test_lane_and_lockstep_schedules_agree_bitwise(ctx, precision):
+    from nbody.lib import set_bh_schedule
+    d = bodies("disc", 30000, seed=17)
+    tree, dd = build(ctx, d, theta=0.5)
+    try:
+        set_bh_schedule(lockstep=True)
+        a = accel(ctx, tree, dd, d["G"], 1e-22, "theta", precision)
+    finally:
+        set_bh_schedule(lockstep=False)
+    b = accel(ctx, tree, dd, d["G"], 1e-22, "theta", precision)
+    for u, v in zip(a, b):
+        np.testing.assert_array_equal(u, v)
