@@ -83,6 +83,45 @@ nb_status nb_naive_accel_range(nb_ctx* ctx, const double* m, const double* x, co
                                uint32_t i_begin, uint32_t i_end, double G, double eps2,
                                nb_precision prec, nb_stream_t stream);
 
+/* Tile configuration of the FP32-compensated pair kernel used by nb_naive_accel (process-wide;
+ * 0..NB_PAIR_CONFIG_COUNT-1, see nb_batch_info for the shapes; 0 = default). */
+#define NB_PAIR_CONFIG_COUNT 6
+nb_status nb_naive_set_pair_config(int config);
+
+/* ---------------------------------------------------------------------------------------------
+ * Batched ensembles (the spec batching form; the reference simulates one system).
+ * Many independent systems of uneven size in concatenated FP64 arrays (system s owns bodies
+ * [sum(counts[0..s)), +counts[s])). Forces use FP32 pair math with compensated accumulation, one
+ * persistent stream-K launch for all systems; integration stays FP64 (nb_leapfrog_* over all
+ * bodies). The batch owns every buffer its launches need, so steps can be captured in a graph.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct nb_batch nb_batch;
+typedef struct nb_graph nb_graph;
+nb_status nb_batch_create(nb_ctx* ctx, uint32_t n_systems, const uint32_t* counts_host,
+                          nb_batch** out);
+nb_status nb_batch_destroy(nb_batch* batch);
+/* Total bodies and the current tile configuration: CTA threads, targets per thread, j-tile. */
+nb_status nb_batch_info(const nb_batch* batch, uint32_t* n_total, int* config, int* threads,
+                        int* targets_per_thread, int* j_tile);
+nb_status nb_batch_set_config(nb_ctx* ctx, nb_batch* batch, int config);
+nb_status nb_batch_naive_accel(nb_ctx* ctx, nb_batch* batch, const double* m, const double* x,
+                               const double* y, const double* z, double* ax, double* ay,
+                               double* az, double G, double eps2, nb_stream_t stream);
+/* Autotuner (synchronous): times every tile configuration on these arrays (reps launches each,
+ * CUDA events), keeps the fastest; ms_per_config (host, NB_PAIR_CONFIG_COUNT entries) optional. */
+nb_status nb_batch_autotune(nb_ctx* ctx, nb_batch* batch, const double* m, const double* x,
+                            const double* y, const double* z, double* ax, double* ay, double* az,
+                            double G, double eps2, int reps, float* ms_per_config, int* chosen);
+/* Captures `steps` leapfrog steps (kick-drift, batch accelerations, kick) of the batch into a
+ * CUDA graph; nb_graph_launch replays them on a stream. */
+nb_status nb_batch_graph_create(nb_ctx* ctx, nb_batch* batch, const double* m, double* x,
+                                double* y, double* z, double* vx, double* vy, double* vz,
+                                double* vhx, double* vhy, double* vhz, double* ax, double* ay,
+                                double* az, double G, double eps2, double dt, int steps,
+                                nb_graph** out);
+nb_status nb_graph_launch(nb_graph* graph, nb_stream_t stream);
+nb_status nb_graph_destroy(nb_graph* graph);
+
 /* ---------------------------------------------------------------------------------------------
  * Leapfrog kick-drift-kick.
  * nb_leapfrog_kick_drift replaces "leapfrog integration part 1" (NaiveAlgorithm.cpp:140-164,

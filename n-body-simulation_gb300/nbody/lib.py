@@ -195,6 +195,17 @@ SIGNATURES.update({
     "nb_bh_count_interactions": [_vp, _vp, _vp, _vp, _vp, _i, _vp, _vp],
     "nb_util_fma_peak": [_vp, _i, C.POINTER(_d)],
     "nb_bh_set_schedule": [_i],
+    "nb_naive_set_pair_config": [_i],
+    "nb_batch_create": [_vp, _u32, _vp, C.POINTER(_vp)],
+    "nb_batch_destroy": [_vp],
+    "nb_batch_info": [_vp, C.POINTER(_u32), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i),
+                      C.POINTER(_i)],
+    "nb_batch_set_config": [_vp, _vp, _i],
+    "nb_batch_naive_accel": [_vp, _vp] + [_vp] * 7 + [_d, _d, _vp],
+    "nb_batch_autotune": [_vp, _vp] + [_vp] * 7 + [_d, _d, _i, _vp, C.POINTER(_i)],
+    "nb_batch_graph_create": [_vp, _vp] + [_vp] * 13 + [_d, _d, _d, _i, C.POINTER(_vp)],
+    "nb_graph_launch": [_vp, _vp],
+    "nb_graph_destroy": [_vp],
 })
 
 
@@ -306,3 +317,82 @@ def util_radix_sort_pairs(ctx: Context, keys, vals, begin_bit=0, end_bit=64, str
 def util_exclusive_scan_u32(ctx: Context, inp, out, stream=None):
     check(load().nb_util_exclusive_scan_u32(ctx.handle, ptr(inp), ptr(out), inp.numel(),
                                             stream_ptr(stream)))
+
+
+def set_naive_pair_config(config: int):
+    check(load().nb_naive_set_pair_config(config))
+
+
+class Batch:
+    """Ensemble of independent systems in concatenated arrays (nb_batch)."""
+
+    def __init__(self, ctx: Context, counts):
+        import numpy as np
+        self.ctx = ctx
+        self.lib = load()
+        self.counts = np.ascontiguousarray(counts, dtype=np.uint32)
+        h = _vp()
+        check(self.lib.nb_batch_create(ctx.handle, len(self.counts), self.counts.ctypes.data,
+                                       C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.nb_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        n, c, t, ip, jt = _u32(), _i(), _i(), _i(), _i()
+        check(self.lib.nb_batch_info(self.handle, C.byref(n), C.byref(c), C.byref(t), C.byref(ip),
+                                     C.byref(jt)))
+        return {"n_total": n.value, "config": c.value, "threads": t.value,
+                "targets_per_thread": ip.value, "j_tile": jt.value}
+
+    def set_config(self, config: int):
+        check(self.lib.nb_batch_set_config(self.ctx.handle, self.handle, config))
+
+    def accel(self, m, x, y, z, ax, ay, az, G, eps2, stream=None):
+        check(self.lib.nb_batch_naive_accel(self.ctx.handle, self.handle, ptr(m), ptr(x), ptr(y),
+                                            ptr(z), ptr(ax), ptr(ay), ptr(az), G, eps2,
+                                            stream_ptr(stream)))
+
+    def autotune(self, m, x, y, z, ax, ay, az, G, eps2, reps=3):
+        ms = (C.c_float * 6)()
+        chosen = _i()
+        check(self.lib.nb_batch_autotune(self.ctx.handle, self.handle, ptr(m), ptr(x), ptr(y),
+                                         ptr(z), ptr(ax), ptr(ay), ptr(az), G, eps2, reps, ms,
+                                         C.byref(chosen)))
+        return chosen.value, list(ms)
+
+    def graph(self, m, pos, vel, vh, acc, G, eps2, dt, steps):
+        h = _vp()
+        check(self.lib.nb_batch_graph_create(self.ctx.handle, self.handle, ptr(m), *map(ptr, pos),
+                                             *map(ptr, vel), *map(ptr, vh), *map(ptr, acc), G,
+                                             eps2, dt, steps, C.byref(h)))
+        return Graph(h)
+
+
+class Graph:
+    def __init__(self, handle):
+        self.lib = load()
+        self.handle = handle
+
+    def launch(self, stream=None):
+        check(self.lib.nb_graph_launch(self.handle, stream_ptr(stream)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.nb_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
