@@ -83,6 +83,13 @@ nb_status nb_naive_accel_range(nb_ctx* ctx, const double* m, const double* x, co
                                uint32_t i_begin, uint32_t i_end, double G, double eps2,
                                nb_precision prec, nb_stream_t stream);
 
+/* FP64 accelerations of listed target bodies: ax[t] for body targets[t] (all DEVICE arrays); the
+ * FP64 GPU oracle for sampled-body force errors at large N. */
+nb_status nb_naive_accel_targets(nb_ctx* ctx, const double* m, const double* x, const double* y,
+                                 const double* z, uint32_t n, const uint32_t* targets,
+                                 uint32_t n_targets, double* ax, double* ay, double* az, double G,
+                                 double eps2, nb_stream_t stream);
+
 /* Tile configuration of the FP32-compensated pair kernel used by nb_naive_accel (process-wide;
  * 0..NB_PAIR_CONFIG_COUNT-1, see nb_batch_info for the shapes; 0 = default). */
 #define NB_PAIR_CONFIG_COUNT 6
@@ -267,6 +274,10 @@ nb_status nb_bh_set_schedule(int lockstep);
 /* Synchronous. */
 nb_status nb_bh_tree_stats(nb_bh_tree* tree, nb_bh_stats* out);
 nb_status nb_bh_export_ref_layout(nb_bh_tree* tree, nb_bh_ref_layout* out);
+/* Per node in DFS order (HOST arrays of node_count entries, any may be NULL): first sorted position
+ * of its bodies, body count, level, body id (NB leaves) or 0xffffffff. */
+nb_status nb_bh_export_node_ranges(nb_bh_tree* tree, uint32_t* first, uint32_t* count,
+                                   uint32_t* level, uint32_t* body);
 /* Sorted body ids (tree DFS order) and per-body leaf depth, HOST arrays of n entries. */
 nb_status nb_bh_export_order(nb_bh_tree* tree, uint32_t* ids_in_dfs_order, uint32_t* leaf_level);
 
@@ -279,6 +290,53 @@ nb_status nb_bh_count_interactions(nb_ctx* ctx, const nb_bh_tree* tree, const do
 /* Synchronous FMA-throughput probe of the current GPU: FP64 (fp64 = 1) or FP32 flop/s (2 per FMA).
  * The measured pipe peaks the pair and traversal kernels are reported against. */
 nb_status nb_util_fma_peak(nb_ctx* ctx, int fp64, double* flops_per_s);
+
+/* ---------------------------------------------------------------------------------------------
+ * Learned opening policy (the spec learned form; no reference counterpart).
+ * Network: 8 features -> 32 -> 32 -> 1 (ReLU), NB_MLP_PARAMS FP32 parameters in the layout
+ * W1[8][32], b1[32], W2[32][32], b2[32], w3[32], b3 (all DEVICE arrays). It predicts
+ * y = log10(worst relative force error of accepting a cell for a 32-body group) / 5.
+ * ------------------------------------------------------------------------------------------- */
+#define NB_MLP_PARAMS 1377
+#define NB_MLP_FEATURES 8
+nb_status nb_mlp_param_count(uint32_t* out);
+/* Mean-squared-error loss and its gradient over rows idx[0..n) (idx NULL: rows 0..n) of X [n][8]
+ * and Y [n]; grad (NB_MLP_PARAMS floats) and loss (1 float) are overwritten. FP32. */
+nb_status nb_mlp_loss_grad(nb_ctx* ctx, const float* params, const float* X, const float* Y,
+                           const uint32_t* idx, uint32_t n, float* grad, float* loss,
+                           nb_stream_t stream);
+/* One Adam step (step = 1, 2, ...) on params with moment buffers m, v (NB_MLP_PARAMS each). */
+nb_status nb_mlp_adam(nb_ctx* ctx, float* params, float* m, float* v, const float* grad,
+                      float lr, float beta1, float beta2, float eps, int step, nb_stream_t stream);
+/* Network outputs for X [n][8]: FP32 CUDA cores, or (bf16_tensor_cores = 1) the BF16 mma.sync
+ * path the traversal uses. */
+nb_status nb_mlp_predict(nb_ctx* ctx, const float* params, const float* X, uint32_t n,
+                         float* out, int bf16_tensor_cores, nb_stream_t stream);
+/* Labelled training pairs from a built tree: a group theta_gen walk samples (32-body group, cell)
+ * pairs (fraction sample_fraction, seeded); for each, features and the label log10(max over the
+ * group of |exact cell force - monopole| / |a_body|) / 5, with |a_body| from ax, ay, az
+ * (reference accelerations). Writes at most max_pairs rows; *count_dev (DEVICE) = pairs found
+ * (may exceed max_pairs). Cells with more than count_cap bodies are not sampled. pairs_out
+ * (optional DEVICE, 2*max_pairs u32) receives each row's (group = first sorted position / 32,
+ * node in DFS order). */
+nb_status nb_bh_generate_pairs(nb_ctx* ctx, const nb_bh_tree* tree, const double* m,
+                               const double* x, const double* y, const double* z,
+                               const double* ax, const double* ay, const double* az, double G,
+                               double eps2, double theta_gen, double sample_fraction,
+                               uint32_t seed, uint32_t count_cap, uint32_t max_pairs,
+                               float* features, float* labels, uint32_t* count_dev,
+                               uint32_t* pairs_out, nb_stream_t stream);
+/* Policy of NB_OPEN_LEARNED: accept a cell when the network predicts an error below tau;
+ * cells with more than count_cap bodies use the group theta rule with theta_fallback. The
+ * traversal reads |a| of the previous step from the ax, ay, az arrays it then overwrites. */
+nb_status nb_bh_set_policy(nb_bh_tree* tree, const float* params_dev, float log10_tau,
+                           double theta_fallback, uint32_t count_cap);
+/* NB_OPEN_LEARNED traversal that also counts body-cell interactions (counters_dev[0]) and
+ * network evaluations (counters_dev[1]) into 2 DEVICE uint64. */
+nb_status nb_bh_accel_learned_counted(nb_ctx* ctx, const nb_bh_tree* tree, const double* x,
+                                      const double* y, const double* z, double* ax, double* ay,
+                                      double* az, double eps2, unsigned long long* counters_dev,
+                                      nb_stream_t stream);
 
 /* Building blocks exposed for tests: stable radix sort of (u64, u32) device pairs on bits
  * [begin_bit, end_bit) and an exclusive scan of u32 device data (out has n+1 entries). These two

@@ -247,13 +247,18 @@ struct ComArgs {
     const uint8_t* node_level;
     const uint32_t *node_first, *node_skip, *node_parent, *node_body, *node_nchild;
     uint32_t *node_arrive, *node_count;
-    double *comx, *comy, *comz, *mass;
+    double *comx, *comy, *comz, *mass, *q;
     NodeRec64* rec64;
     NodeRec32* rec32;
+    NodeAux* aux;
+    const uint32_t* node_first_pos;
+    uint32_t* children;
+    float4* sorted4;
 };
 
 __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double cy, double cz,
-                              double sm, int level, uint32_t skip, uint32_t body) {
+                              double sm, double qsum, uint32_t count, int level, uint32_t skip,
+                              uint32_t body) {
     const double edge = ldexp(A.box[6], -level);
     NodeRec64 r;
     r.cx = sm != 0 ? __ddiv_rn(cx, sm) : 0.0;  // massless cells: finite centre (never used)
@@ -280,6 +285,21 @@ __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double 
     q.body = body;
     q.level = (uint32_t)level;
     A.rec32[idx] = q;
+    // spread^2 = sum m |x-o|^2 / M - |c-o|^2 (o = box centre, which keeps both terms small)
+    NodeAux x;
+    if (sm != 0) {
+        const double ox = A.box[0] + A.box[6] / 2, oy = A.box[1] + A.box[6] / 2,
+                     oz = A.box[2] + A.box[6] / 2;
+        const double gx = r.cx - ox, gy = r.cy - oy, gz = r.cz - oz;
+        const double s2 = qsum / sm - (gx * gx + gy * gy + gz * gz);
+        x.spread = (float)sqrt(s2 > 0 ? s2 : 0.0);
+    } else {
+        x.spread = 0.f;
+    }
+    x.count = count;
+    x.first = A.node_first_pos[idx];
+    x.edge = (float)edge;
+    A.aux[idx] = x;
 }
 
 __global__ void com_kernel(ComArgs A) {
@@ -289,12 +309,18 @@ __global__ void com_kernel(ComArgs A) {
     const uint32_t b = A.ids[p];
     const double mb = A.m[b];
     const double cx = __dmul_rn(A.x[b], mb), cy = __dmul_rn(A.y[b], mb), cz = __dmul_rn(A.z[b], mb);
+    const double ox = A.box[0] + A.box[6] / 2, oy = A.box[1] + A.box[6] / 2,
+                 oz = A.box[2] + A.box[6] / 2;
+    const double rx = A.x[b] - ox, ry = A.y[b] - oy, rz = A.z[b] - oz;
+    const double qb = mb * (rx * rx + ry * ry + rz * rz);
     A.comx[idx] = cx;
     A.comy[idx] = cy;
     A.comz[idx] = cz;
     A.mass[idx] = mb;
+    A.q[idx] = qb;
     A.node_count[idx] = 1;
-    write_records(A, idx, cx, cy, cz, mb, A.node_level[idx], A.node_skip[idx], b);
+    A.sorted4[p] = make_float4((float)rx, (float)ry, (float)rz, (float)(A.G * mb));
+    write_records(A, idx, cx, cy, cz, mb, qb, 1, A.node_level[idx], A.node_skip[idx], b);
     uint32_t cur = A.node_parent[idx];
     while (cur != NB_NONE) {
         __threadfence();
@@ -306,11 +332,19 @@ __global__ void com_kernel(ComArgs A) {
         for (int o = 0; o < 8; ++o) slot[o] = NB_NONE;
         const uint32_t end = A.node_skip[cur];
         uint32_t c = cur + 1;
+        uint32_t list[8];
+        int nch = 0;
         for (int k = 0; k < 8 && c < end; ++k) {
             slot[nb_octant_of_visit(digit_at(A.key0, A.key1, A.node_first[c], L))] = c;
+            list[nch++] = c;
             c = A.node_skip[c];
         }
-        double sx = 0, sy = 0, sz = 0, sm = 0;
+        uint4* out = reinterpret_cast<uint4*>(A.children + (size_t)cur * 8);
+        out[0] = make_uint4(list[0], nch > 1 ? list[1] : NB_NONE, nch > 2 ? list[2] : NB_NONE,
+                            nch > 3 ? list[3] : NB_NONE);
+        out[1] = make_uint4(nch > 4 ? list[4] : NB_NONE, nch > 5 ? list[5] : NB_NONE,
+                            nch > 6 ? list[6] : NB_NONE, nch > 7 ? list[7] : NB_NONE);
+        double sx = 0, sy = 0, sz = 0, sm = 0, sq = 0;
         uint32_t count = 0;
 #pragma unroll
         for (int o = 0; o < 8; ++o) {
@@ -320,14 +354,16 @@ __global__ void com_kernel(ComArgs A) {
             sy = __dadd_rn(sy, __ldcg(&A.comy[ch]));
             sz = __dadd_rn(sz, __ldcg(&A.comz[ch]));
             sm = __dadd_rn(sm, __ldcg(&A.mass[ch]));
+            sq += __ldcg(&A.q[ch]);
             count += __ldcg(&A.node_count[ch]);
         }
         A.comx[cur] = sx;
         A.comy[cur] = sy;
         A.comz[cur] = sz;
         A.mass[cur] = sm;
+        A.q[cur] = sq;
         A.node_count[cur] = count;
-        write_records(A, cur, sx, sy, sz, sm, L, end, NB_NONE);
+        write_records(A, cur, sx, sy, sz, sm, sq, count, L, end, NB_NONE);
         cur = A.node_parent[cur];
     }
 }
@@ -379,6 +415,10 @@ void carve(nb_bh_tree* t, Carver& c) {
     t->node_mass = c.take<double>(cap);
     t->rec64 = c.take<NodeRec64>(cap);
     t->rec32 = c.take<NodeRec32>(cap);
+    t->node_q = c.take<double>(cap);
+    t->aux = c.take<NodeAux>(cap);
+    t->children = c.take<uint32_t>(cap * 8);
+    t->sorted4 = c.take<float4>(n);
 }
 
 }  // namespace
@@ -510,6 +550,11 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     A.mass = t->node_mass;
     A.rec64 = t->rec64;
     A.rec32 = t->rec32;
+    A.q = t->node_q;
+    A.aux = t->aux;
+    A.node_first_pos = t->node_first;
+    A.children = t->children;
+    A.sorted4 = t->sorted4;
     com_kernel<<<grid, BH_THREADS, 0, s>>>(A);
     NB_TRY(nb::check_launch("com_kernel"));
     t->built = true;

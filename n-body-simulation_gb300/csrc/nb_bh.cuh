@@ -28,6 +28,14 @@ struct __align__(16) NodeRec32 {
     uint32_t skip, body, level;
 };
 
+// Extra per-node data of the learned opening policy.
+struct __align__(16) NodeAux {
+    float spread;    // mass-weighted rms distance of the cell's bodies from its centre of mass
+    uint32_t count;  // bodies in the cell
+    uint32_t first;  // first sorted position of the cell's bodies (they are contiguous)
+    float edge;
+};
+
 struct nb_bh_tree {
     uint32_t n_max = 0;
     uint32_t n = 0;
@@ -56,6 +64,15 @@ struct nb_bh_tree {
     double *node_comx = nullptr, *node_comy = nullptr, *node_comz = nullptr, *node_mass = nullptr;
     NodeRec64* rec64 = nullptr;
     NodeRec32* rec32 = nullptr;
+    double* node_q = nullptr;  // sum of m |x - box centre|^2 (for the spread)
+    NodeAux* aux = nullptr;
+    uint32_t* children = nullptr;  // 8 per node: children in visit order, NB_NONE padded
+    float4* sorted4 = nullptr;     // per sorted position: position relative to the box centre, G*m
+    // learned opening policy (device parameters, see nb_learned.cu)
+    const float* policy = nullptr;
+    float policy_log_tau = 0.f;
+    float policy_theta = 0.5f;
+    uint32_t policy_count_cap = 8192;
 };
 
 // Digit maps between the reference's octant index o = 4*(y>mid) + 2*(x>mid) + (z<mid) and the

@@ -202,4 +202,17 @@ nb_status nb_bh_export_ref_layout(nb_bh_tree* t, nb_bh_ref_layout* out) {
     return NB_OK;
 }
 
+nb_status nb_bh_export_node_ranges(nb_bh_tree* t, uint32_t* first, uint32_t* count,
+                                   uint32_t* level, uint32_t* body) {
+    HostTree h;
+    NB_TRY(fetch_tree(t, h, true));
+    for (uint32_t k = 0; k < h.nodes; ++k) {
+        if (first) first[k] = h.first[k];
+        if (count) count[k] = h.count[k];
+        if (level) level[k] = h.level[k];
+        if (body) body[k] = h.body[k];
+    }
+    return NB_OK;
+}
+
 }  // extern "C"

@@ -408,6 +408,12 @@ int g_lockstep = 0;
 
 }  // namespace
 
+namespace nb {
+nb_status launch_learned(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const double* y,
+                         const double* z, double* ax, double* ay, double* az, double eps2,
+                         unsigned long long* counters, cudaStream_t s);
+}
+
 extern "C" {
 
 nb_status nb_bh_set_schedule(int lockstep) {
@@ -477,7 +483,11 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
                 break;
         }
     } else if (opening == NB_OPEN_LEARNED) {
-        return nb::set_error(NB_ERR_UNSUPPORTED, "nb_bh_accel: NB_OPEN_LEARNED needs a policy");
+        if (prec != NB_F32C)
+            return nb::set_error(NB_ERR_UNSUPPORTED, "nb_bh_accel: NB_OPEN_LEARNED runs in NB_F32C");
+        if (G != t->G)
+            return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: G differs from the build's");
+        return nb::launch_learned(ctx, t, x, y, z, ax, ay, az, eps2, nullptr, s);
     }
     return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: unknown opening %d / precision %d",
                          (int)opening, (int)prec);
@@ -497,6 +507,17 @@ nb_status nb_bh_count_interactions(nb_ctx* ctx, const nb_bh_tree* t, const doubl
         t->rec64, t->info, t->ids, x, y, z, t->n, t->params.theta,
         opening == NB_OPEN_THETA_GROUP ? 1 : 0, out_dev);
     return nb::check_launch("bh_count_kernel");
+}
+
+nb_status nb_bh_accel_learned_counted(nb_ctx* ctx, const nb_bh_tree* t, const double* x,
+                                     const double* y, const double* z, double* ax, double* ay,
+                                     double* az, double eps2, unsigned long long* counters_dev,
+                                     nb_stream_t stream) {
+    NB_CHECK_CTX(ctx);
+    if (!t || !t->built) return nb::set_error(NB_ERR_NOT_BUILT, "tree not built");
+    if (!counters_dev) return nb::set_error(NB_ERR_INVALID_ARG, "null counters");
+    NB_CUDA_TRY(cudaMemsetAsync(counters_dev, 0, 2 * sizeof(unsigned long long), (cudaStream_t)stream));
+    return nb::launch_learned(ctx, t, x, y, z, ax, ay, az, eps2, counters_dev, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -1,0 +1,829 @@
+// nb_learned.cu -- learned opening policy for the Barnes-Hut traversal.
+//
+// A small MLP (8 -> 32 -> 32 -> 1, ReLU) predicts, for a group of 32 bodies adjacent in tree
+// order and a cell, y = log10(max over the group of |F_exact - F_monopole| / |a_body|) / 5: the
+// worst relative force error that accepting the cell's monopole would add to the group. The
+// traversal accepts the cell when y < log10(tau)/5.
+//
+//  * Labels come from the method itself (nb_bh_generate_pairs): a theta-rule walk samples
+//    (group, cell) pairs, and for each pair one warp computes the exact cell force on its 32
+//    bodies by direct summation over the cell's bodies (contiguous in tree order) against the
+//    cell's monopole.
+//  * Training (nb_mlp_loss_grad, nb_mlp_adam): FP32 forward/backward kernels, MSE loss, Adam.
+//  * Inference (nb_bh_accel with NB_OPEN_LEARNED): each warp keeps a stack of cells in shared
+//    memory, pops up to 16 at a time and scores them with BF16 tensor-core mma.sync.m16n8k16
+//    (FP32 accumulate); each layer's accumulator fragments are reused in registers as the next
+//    layer's A fragments. Body leaves are always accepted, cells that may overlap the group are
+//    always opened, and cells with more bodies than the training range fall back to the group
+//    theta rule.
+#include <cuda_bf16.h>
+
+#include "nb_bh.cuh"
+
+namespace {
+
+// parameter layout (FP32): W1[8][32], b1[32], W2[32][32], b2[32], w3[32], b3
+constexpr int P_W1 = 0, P_B1 = 256, P_W2 = 288, P_B2 = 1312, P_W3 = 1344, P_B3 = 1376;
+constexpr int P_COUNT = 1377;
+constexpr int NF = 8;
+constexpr float SQRT3 = 1.7320508f;
+
+struct GroupGeo {
+    float cx, cy, cz, r, a_ref;
+    float hx, hy, hz;  // half extents of the group's bounding box
+};
+
+__device__ __forceinline__ float warp_min(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Group geometry from the lanes' FP32 positions (relative to the box centre): bounding-box
+// centre, radius, and the weakest previous acceleration of the group.
+__device__ GroupGeo group_geo(bool valid, float px, float py, float pz, float a_prev) {
+    const float inf = __int_as_float(0x7f800000);
+    GroupGeo g;
+    const float lx = warp_min(valid ? px : inf), hx = warp_max(valid ? px : -inf);
+    const float ly = warp_min(valid ? py : inf), hy = warp_max(valid ? py : -inf);
+    const float lz = warp_min(valid ? pz : inf), hz = warp_max(valid ? pz : -inf);
+    g.cx = 0.5f * (lx + hx);
+    g.cy = 0.5f * (ly + hy);
+    g.cz = 0.5f * (lz + hz);
+    g.hx = 0.5f * (hx - lx);
+    g.hy = 0.5f * (hy - ly);
+    g.hz = 0.5f * (hz - lz);
+    const float dx = px - g.cx, dy = py - g.cy, dz = pz - g.cz;
+    g.r = warp_max(valid ? sqrtf(dx * dx + dy * dy + dz * dz) : 0.f);
+    g.a_ref = fmaxf(warp_min(valid ? a_prev : inf), 1e-30f);
+    return g;
+}
+
+// The 8 features of a (group, cell) pair and the cell's class: 0 = decide with the network,
+// 1 = body leaf (accept), 2 = may overlap the group (open), 3 = outside the training range
+// (theta rule). gap = the smallest distance from a member of the group to the cell's centre of
+// mass; d = distance from the group's box centre.
+__device__ __forceinline__ int cell_features(const NodeRec32& r, const NodeAux& x,
+                                             const GroupGeo& g, float gap, uint32_t count_cap,
+                                             float* f) {
+    if (r.body != NB_NONE) return 1;
+    const float e = x.edge;
+    if (gap <= SQRT3 * e) return 2;
+    if (x.count > count_cap) return 3;
+    const float dx = r.cx - g.cx, dy = r.cy - g.cy, dz = r.cz - g.cz;
+    const float d = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+    f[0] = __log2f(d / e) * 0.25f;
+    f[1] = x.spread / e;
+    f[2] = __log2f((float)x.count) * 0.0625f;
+    f[3] = (float)r.level * 0.0625f;
+    f[4] = g.r / d;
+    f[5] = __log10f(fmaxf(r.gm, 1e-37f) / (gap * gap * g.a_ref)) * 0.25f;
+    f[6] = __log2f(gap / e) * 0.25f;
+    f[7] = x.spread / gap;
+    return 0;
+}
+
+// Smallest distance from a valid lane's body to (cx, cy, cz), over the whole warp.
+__device__ __forceinline__ float warp_min_dist(bool valid, float px, float py, float pz, float cx,
+                                               float cy, float cz) {
+    const float dx = cx - px, dy = cy - py, dz = cz - pz;
+    const float inf = __int_as_float(0x7f800000);
+    return sqrtf(warp_min(valid ? fmaf(dx, dx, fmaf(dy, dy, dz * dz)) : inf));
+}
+
+// ---------------------------------------------------------------------------------------------
+// BF16 tensor-core MLP over 16 cells (mma.sync.m16n8k16, FP32 accumulate)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mma16816(float* c, uint32_t a0, uint32_t a1, uint32_t a2,
+                                         uint32_t a3, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// Weight fragments of one lane (g = lane/4, t = lane%4).
+struct MlpFrags {
+    uint32_t w1[4];        // layer 1, n-tile nt: W1[2t..2t+1][nt*8+g] (k rows 8..15 are zero)
+    uint32_t w2[2][4][2];  // layer 2, k-step ks, n-tile nt
+    uint32_t w3[2][2];     // layer 3 (output column 0 only: lanes with g == 0)
+    float b1[4][2], b2[4][2], b3;
+};
+
+__device__ void load_frags(const float* __restrict__ P, int lane, MlpFrags& F) {
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        const int o = nt * 8 + g;
+        F.w1[nt] = pack_bf16(P[P_W1 + (2 * t) * 32 + o], P[P_W1 + (2 * t + 1) * 32 + o]);
+        F.b1[nt][0] = P[P_B1 + nt * 8 + 2 * t];
+        F.b1[nt][1] = P[P_B1 + nt * 8 + 2 * t + 1];
+        F.b2[nt][0] = P[P_B2 + nt * 8 + 2 * t];
+        F.b2[nt][1] = P[P_B2 + nt * 8 + 2 * t + 1];
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks) {
+            const int k0 = ks * 16 + 2 * t;
+            F.w2[ks][nt][0] = pack_bf16(P[P_W2 + k0 * 32 + o], P[P_W2 + (k0 + 1) * 32 + o]);
+            F.w2[ks][nt][1] = pack_bf16(P[P_W2 + (k0 + 8) * 32 + o], P[P_W2 + (k0 + 9) * 32 + o]);
+        }
+    }
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+        const int k0 = ks * 16 + 2 * t;
+        F.w3[ks][0] = g == 0 ? pack_bf16(P[P_W3 + k0], P[P_W3 + k0 + 1]) : 0u;
+        F.w3[ks][1] = g == 0 ? pack_bf16(P[P_W3 + k0 + 8], P[P_W3 + k0 + 9]) : 0u;
+    }
+    F.b3 = P[P_B3];
+}
+
+// Scores of the 16 feature rows in smem (row-major [16][16] bf16, columns 8..15 zero); returns
+// the score of row (lane & 15).
+__device__ float mlp16(const __nv_bfloat16* __restrict__ feat, int lane, const MlpFrags& F) {
+    const int g = lane >> 2, t = lane & 3;
+    const uint32_t* row = reinterpret_cast<const uint32_t*>(feat);  // 8 u32 per row
+    const uint32_t a0 = row[g * 8 + t], a1 = row[(g + 8) * 8 + t];
+    float c1[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        c1[nt][0] = F.b1[nt][0];
+        c1[nt][1] = F.b1[nt][1];
+        c1[nt][2] = F.b1[nt][0];
+        c1[nt][3] = F.b1[nt][1];
+        mma16816(c1[nt], a0, a1, 0u, 0u, F.w1[nt], 0u);
+    }
+    uint32_t h1[2][4];
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+        h1[ks][0] = pack_bf16(fmaxf(c1[2 * ks][0], 0.f), fmaxf(c1[2 * ks][1], 0.f));
+        h1[ks][1] = pack_bf16(fmaxf(c1[2 * ks][2], 0.f), fmaxf(c1[2 * ks][3], 0.f));
+        h1[ks][2] = pack_bf16(fmaxf(c1[2 * ks + 1][0], 0.f), fmaxf(c1[2 * ks + 1][1], 0.f));
+        h1[ks][3] = pack_bf16(fmaxf(c1[2 * ks + 1][2], 0.f), fmaxf(c1[2 * ks + 1][3], 0.f));
+    }
+    float c2[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        c2[nt][0] = F.b2[nt][0];
+        c2[nt][1] = F.b2[nt][1];
+        c2[nt][2] = F.b2[nt][0];
+        c2[nt][3] = F.b2[nt][1];
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks)
+            mma16816(c2[nt], h1[ks][0], h1[ks][1], h1[ks][2], h1[ks][3], F.w2[ks][nt][0],
+                     F.w2[ks][nt][1]);
+    }
+    uint32_t h2[2][4];
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+        h2[ks][0] = pack_bf16(fmaxf(c2[2 * ks][0], 0.f), fmaxf(c2[2 * ks][1], 0.f));
+        h2[ks][1] = pack_bf16(fmaxf(c2[2 * ks][2], 0.f), fmaxf(c2[2 * ks][3], 0.f));
+        h2[ks][2] = pack_bf16(fmaxf(c2[2 * ks + 1][0], 0.f), fmaxf(c2[2 * ks + 1][1], 0.f));
+        h2[ks][3] = pack_bf16(fmaxf(c2[2 * ks + 1][2], 0.f), fmaxf(c2[2 * ks + 1][3], 0.f));
+    }
+    float c3[4] = {F.b3, F.b3, F.b3, F.b3};
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks)
+        mma16816(c3, h2[ks][0], h2[ks][1], h2[ks][2], h2[ks][3], F.w3[ks][0], F.w3[ks][1]);
+    // row r's score sits in lane 4*(r%8): c3[0] for r < 8, c3[2] for r >= 8
+    const int r = lane & 15;
+    const float v0 = __shfl_sync(0xffffffffu, c3[0], 4 * (r & 7));
+    const float v2 = __shfl_sync(0xffffffffu, c3[2], 4 * (r & 7));
+    return r < 8 ? v0 : v2;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Learned traversal
+// ---------------------------------------------------------------------------------------------
+constexpr int LT_WARPS = 4;
+constexpr int LT_THREADS = LT_WARPS * 32;
+constexpr int LT_CAP = 1024;  // stack entries per warp
+constexpr int LT_BATCH = 16;
+constexpr uint32_t LT_DIRECT = 16;  // opened cells up to this many bodies: direct sums
+constexpr int LT_LIST = 512;        // interaction list entries per warp
+
+// Sum of the interactions in list[0..count) for one body; 4 independent accumulators. An entry
+// at zero distance (the body itself) contributes nothing.
+__device__ __forceinline__ void flush_list(const float4* __restrict__ list, int count, float px,
+                                           float py, float pz, float eps2, float& ox, float& oy,
+                                           float& oz) {
+    float ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
+    int j = 0;
+    for (; j + 4 <= count; j += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float4 e = list[j + u];
+            const float dx = e.x - px, dy = e.y - py, dz = e.z - pz;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float inv = rsqrtf(r2 + eps2);
+            const float w = r2 > 0.f ? e.w * inv * inv * inv : 0.f;
+            ax[u] = fmaf(dx, w, ax[u]);
+            ay[u] = fmaf(dy, w, ay[u]);
+            az[u] = fmaf(dz, w, az[u]);
+        }
+    }
+    for (; j < count; ++j) {
+        const float4 e = list[j];
+        const float dx = e.x - px, dy = e.y - py, dz = e.z - pz;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float inv = rsqrtf(r2 + eps2);
+        const float w = r2 > 0.f ? e.w * inv * inv * inv : 0.f;
+        ax[0] = fmaf(dx, w, ax[0]);
+        ay[0] = fmaf(dy, w, ay[0]);
+        az[0] = fmaf(dz, w, az[0]);
+    }
+    ox = (ax[0] + ax[1]) + (ax[2] + ax[3]);
+    oy = (ay[0] + ay[1]) + (ay[2] + ay[3]);
+    oz = (az[0] + az[1]) + (az[2] + az[3]);
+}
+
+__global__ void __launch_bounds__(LT_THREADS)
+bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__ aux,
+                  const uint32_t* __restrict__ children, const float4* __restrict__ sorted4,
+                  const uint32_t* __restrict__ info,
+                  const uint32_t* __restrict__ ids, const double* __restrict__ x,
+                  const double* __restrict__ y, const double* __restrict__ z,
+                  const double* __restrict__ box, uint32_t n,
+                  const float* __restrict__ params, float log_tau_scaled, float theta2,
+                  uint32_t count_cap, float eps2, double* __restrict__ ax,
+                  double* __restrict__ ay, double* __restrict__ az,
+                  unsigned long long* __restrict__ counters, uint32_t* __restrict__ err_word) {
+    __shared__ uint32_t stack[LT_WARPS][LT_CAP];
+    __shared__ __align__(16) __nv_bfloat16 feat[LT_WARPS][LT_BATCH][16];
+    __shared__ float4 gpos[LT_WARPS][32];
+    __shared__ float4 ilist[LT_WARPS][LT_LIST];
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    const uint32_t gw = blockIdx.x * LT_WARPS + wi;
+    if (gw * 32 >= n) return;  // whole warp past the end
+    const uint32_t p = gw * 32 + lane;
+    const bool valid = p < n;
+    const uint32_t me = valid ? ids[p] : NB_NONE;
+    const double ox = box[0] + box[6] / 2, oy = box[1] + box[6] / 2, oz = box[2] + box[6] / 2;
+    float px = 0, py = 0, pz = 0, a_prev = 0;
+    if (valid) {
+        px = (float)(x[me] - ox);
+        py = (float)(y[me] - oy);
+        pz = (float)(z[me] - oz);
+        const double a2 = ax[me] * ax[me] + ay[me] * ay[me] + az[me] * az[me];
+        a_prev = (float)sqrt(a2);
+    }
+    const GroupGeo G = group_geo(valid, px, py, pz, a_prev);
+    const float inf = __int_as_float(0x7f800000);
+    gpos[wi][lane] = valid ? make_float4(px, py, pz, 0.f) : make_float4(inf, inf, inf, 0.f);
+    MlpFrags F;
+    load_frags(params, lane, F);
+    uint32_t* st = stack[wi];
+    __nv_bfloat16* fm = &feat[wi][0][0];
+    for (int k = lane; k < LT_BATCH * 16; k += 32) fm[k] = __float2bfloat16(0.f);
+    if (lane == 0) st[0] = 0;
+    int top = 1;
+    float hx = 0, hy = 0, hz = 0, lx = 0, ly = 0, lz = 0;
+    int list_n = 0;
+    unsigned long long n_acc = 0, n_mlp = 0;
+    __syncwarp();
+    while (top > 0) {
+        int B = min(LT_BATCH, top);
+        B = min(B, (LT_CAP - top) / 7);
+        if (B <= 0) {  // cannot pop without risking overflow: report and stop
+            if (lane == 0) atomicOr(err_word, NB_DEVERR_STACK);
+            break;
+        }
+        uint32_t node = 0;
+        if (lane < B) node = st[top - 1 - lane];
+        __syncwarp();
+        top -= B;
+        // lanes i and i+16 load cell i and each scan half of the group for the smallest distance
+        const int ci = lane & 15;
+        const uint32_t cnode = __shfl_sync(0xffffffffu, node, ci);
+        NodeRec32 r{};
+        NodeAux xa{};
+        float m2 = inf;
+        if (ci < B) {
+            r = rec[cnode];
+            const int j0 = (lane >> 4) * 16;
+#pragma unroll 4
+            for (int j = j0; j < j0 + 16; ++j) {
+                const float4 q = gpos[wi][j];
+                const float dx = r.cx - q.x, dy = r.cy - q.y, dz = r.cz - q.z;
+                m2 = fminf(m2, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+            }
+        }
+        m2 = fminf(m2, __shfl_xor_sync(0xffffffffu, m2, 16));
+        const float gap = sqrtf(m2);
+        int cls = 1;
+        if (lane < B) {
+            xa = aux[node];
+            float f[NF];
+            cls = cell_features(r, xa, G, gap, count_cap, f);
+            if (cls == 0) {
+#pragma unroll
+                for (int q = 0; q < NF; ++q) fm[lane * 16 + q] = __float2bfloat16(f[q]);
+            }
+        }
+        const bool need = lane < B && cls == 0;
+        const unsigned need_mask = __ballot_sync(0xffffffffu, need);
+        float score = 0.f;
+        if (need_mask) {
+            __syncwarp();
+            score = mlp16(fm, lane, F);
+            n_mlp += __popc(need_mask);
+            __syncwarp();
+        }
+        bool accept = false;
+        if (lane < B) {
+            if (cls == 1) accept = true;
+            else if (cls == 0) accept = score < log_tau_scaled;
+            else if (cls == 3)  // group theta rule on the distance to the group's box
+                accept = gap > 0 && r.edge2 < theta2 * gap * gap;
+        }
+        // accepted monopoles and the bodies of opened cells of at most LT_DIRECT bodies go to the
+        // warp's interaction list, which all lanes sum when it fills
+        const bool direct = lane < B && !accept && xa.count <= LT_DIRECT;
+        const unsigned omask = __ballot_sync(0xffffffffu, lane < B && !accept && !direct);
+        const uint32_t dcount = direct ? xa.count : 0u;
+        uint32_t slots = (accept && lane < B ? 1u : 0u) + dcount;
+        uint32_t pos = slots;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, pos, o);
+            if (lane >= o) pos += v;
+        }
+        const uint32_t batch_total = __shfl_sync(0xffffffffu, pos, 31);
+        pos -= slots;
+        if (list_n + (int)batch_total > LT_LIST) {  // make room: sum the list so far
+            __syncwarp();
+            float fx, fy, fz;
+            flush_list(ilist[wi], list_n, px, py, pz, eps2, fx, fy, fz);
+            if (valid) {
+                float sh = hx + fx, bp = sh - hx;
+                lx += (hx - (sh - bp)) + (fx - bp);
+                hx = sh;
+                sh = hy + fy;
+                bp = sh - hy;
+                ly += (hy - (sh - bp)) + (fy - bp);
+                hy = sh;
+                sh = hz + fz;
+                bp = sh - hz;
+                lz += (hz - (sh - bp)) + (fz - bp);
+                hz = sh;
+            }
+            list_n = 0;
+            __syncwarp();
+        }
+        if (lane < B && accept) ilist[wi][list_n + pos] = make_float4(r.cx, r.cy, r.cz, r.gm);
+        for (uint32_t j = 0; j < dcount; ++j)
+            ilist[wi][list_n + pos + (accept && lane < B ? 1u : 0u) + j] = sorted4[xa.first + j];
+        list_n += (int)batch_total;
+        n_acc += batch_total;
+        __syncwarp();
+        // push the children of opened cells (8-entry child lists, NB_NONE padded)
+        uint4 c0 = make_uint4(NB_NONE, NB_NONE, NB_NONE, NB_NONE), c1 = c0;
+        uint32_t nchild = 0;
+        if ((omask >> lane) & 1u) {
+            const uint4* cl = reinterpret_cast<const uint4*>(children + (size_t)node * 8);
+            c0 = cl[0];
+            c1 = cl[1];
+            const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+#pragma unroll
+            for (int q = 0; q < 8; ++q) nchild += v[q] != NB_NONE;
+        }
+        uint32_t off = nchild;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, off, o);
+            if (lane >= o) off += v;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, off, 31);
+        off -= nchild;
+        if (nchild) {
+            const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q < (int)nchild) st[top + off + q] = v[q];
+        }
+        top += (int)total;
+        __syncwarp();
+    }
+    __syncwarp();
+    float fx, fy, fz;
+    flush_list(ilist[wi], list_n, px, py, pz, eps2, fx, fy, fz);
+    if (valid) {
+        ax[me] = ((double)hx + (double)lx) + (double)fx;
+        ay[me] = ((double)hy + (double)ly) + (double)fy;
+        az[me] = ((double)hz + (double)lz) + (double)fz;
+    }
+    const unsigned valid_lanes = __popc(__ballot_sync(0xffffffffu, valid));
+    if (counters && lane == 0) {
+        atomicAdd(&counters[0], n_acc * (unsigned long long)valid_lanes);
+        atomicAdd(&counters[1], n_mlp);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Label generation
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t hash32(uint32_t a) {
+    a ^= a >> 16;
+    a *= 0x7feb352dU;
+    a ^= a >> 15;
+    a *= 0x846ca68bU;
+    a ^= a >> 16;
+    return a;
+}
+
+// Group-rule walk with theta_gen; records sampled (group, cell) pairs of the network's class 0.
+__global__ void __launch_bounds__(128)
+pairs_collect_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__ aux,
+                     const uint32_t* __restrict__ info, const uint32_t* __restrict__ ids,
+                     const double* __restrict__ x, const double* __restrict__ y,
+                     const double* __restrict__ z, const double* __restrict__ ax,
+                     const double* __restrict__ ay, const double* __restrict__ az,
+                     const double* __restrict__ box, uint32_t n, float theta2, uint32_t count_cap,
+                     uint32_t threshold, uint32_t seed, uint2* __restrict__ out,
+                     uint32_t max_pairs, unsigned int* __restrict__ counter) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw * 32 >= n) return;
+    const uint32_t p = gw * 32 + lane;
+    const bool valid = p < n;
+    const uint32_t me = valid ? ids[p] : NB_NONE;
+    const double ox = box[0] + box[6] / 2, oy = box[1] + box[6] / 2, oz = box[2] + box[6] / 2;
+    float px = 0, py = 0, pz = 0, a_prev = 0;
+    if (valid) {
+        px = (float)(x[me] - ox);
+        py = (float)(y[me] - oy);
+        pz = (float)(z[me] - oz);
+        a_prev = (float)sqrt(ax[me] * ax[me] + ay[me] * ay[me] + az[me] * az[me]);
+    }
+    const GroupGeo G = group_geo(valid, px, py, pz, a_prev);
+    const uint32_t nn = info[0];
+    uint32_t k = 0;
+    while (k < nn) {
+        const NodeRec32 r = rec[k];
+        if (r.body != NB_NONE) {
+            k = r.skip;
+            continue;
+        }
+        const NodeAux xa = aux[k];
+        const float gap = warp_min_dist(valid, px, py, pz, r.cx, r.cy, r.cz);
+        float f[NF];
+        const int cls = cell_features(r, xa, G, gap, count_cap, f);
+        if (cls == 0 && lane == 0 && hash32(k * 2654435761u ^ gw ^ seed) < threshold) {
+            const unsigned int slot = atomicAdd(counter, 1u);
+            if (slot < max_pairs) out[slot] = make_uint2(gw, k);
+        }
+        const bool open = cls == 2 || !(gap > 0 && r.edge2 < theta2 * gap * gap);
+        k = open ? k + 1 : r.skip;
+    }
+}
+
+// One warp per recorded pair: features, and the label from an exact direct sum over the cell.
+__global__ void __launch_bounds__(128)
+pairs_label_kernel(const NodeRec32* __restrict__ rec, const NodeRec64* __restrict__ rec64,
+                   const NodeAux* __restrict__ aux, const uint32_t* __restrict__ ids,
+                   const double* __restrict__ m, const double* __restrict__ x,
+                   const double* __restrict__ y, const double* __restrict__ z,
+                   const double* __restrict__ ax, const double* __restrict__ ay,
+                   const double* __restrict__ az, const double* __restrict__ box, uint32_t n,
+                   double G, float eps2, uint32_t count_cap, const uint2* __restrict__ pairs,
+                   const unsigned int* __restrict__ counter, uint32_t max_pairs,
+                   float* __restrict__ features, float* __restrict__ labels) {
+    __shared__ float4 chunk[4][32];
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    const uint32_t total = min(*counter, max_pairs);
+    for (uint32_t q = blockIdx.x * 4 + wi; q < total; q += gridDim.x * 4) {
+        const uint2 pr = pairs[q];
+        const uint32_t p = pr.x * 32 + lane;
+        const bool valid = p < n;
+        const uint32_t me = valid ? ids[p] : NB_NONE;
+        const double ox = box[0] + box[6] / 2, oy = box[1] + box[6] / 2, oz = box[2] + box[6] / 2;
+        double bx = 0, by = 0, bz = 0;
+        float px = 0, py = 0, pz = 0, a_b = 0;
+        if (valid) {
+            bx = x[me];
+            by = y[me];
+            bz = z[me];
+            px = (float)(bx - ox);
+            py = (float)(by - oy);
+            pz = (float)(bz - oz);
+            a_b = (float)sqrt(ax[me] * ax[me] + ay[me] * ay[me] + az[me] * az[me]);
+        }
+        const GroupGeo Gg = group_geo(valid, px, py, pz, a_b);
+        const NodeRec32 r = rec[pr.y];
+        const NodeAux xa = aux[pr.y];
+        const float gap = warp_min_dist(valid, px, py, pz, r.cx, r.cy, r.cz);
+        float f[NF];
+        cell_features(r, xa, Gg, gap, count_cap, f);
+        // exact cell force on each lane's body; positions relative to the group's first valid
+        // body in FP64 before rounding, so close pairs keep their digits
+        const double gx = __shfl_sync(0xffffffffu, bx, 0), gy = __shfl_sync(0xffffffffu, by, 0),
+                     gz = __shfl_sync(0xffffffffu, bz, 0);
+        const float qx = (float)(bx - gx), qy = (float)(by - gy), qz = (float)(bz - gz);
+        float fx = 0, fy = 0, fz = 0;
+        for (uint32_t base = 0; base < xa.count; base += 32) {
+            const uint32_t j = base + lane;
+            if (j < xa.count) {
+                const uint32_t b = ids[xa.first + j];
+                chunk[wi][lane] = make_float4((float)(x[b] - gx), (float)(y[b] - gy),
+                                              (float)(z[b] - gz), (float)(G * m[b]));
+            }
+            __syncwarp();
+            const uint32_t cnt = min(32u, xa.count - base);
+            float cxs = 0, cys = 0, czs = 0;
+            for (uint32_t jj = 0; jj < cnt; ++jj) {
+                const float4 s = chunk[wi][jj];
+                const float dx = s.x - qx, dy = s.y - qy, dz = s.z - qz;
+                const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
+                const float w = s.w * inv * inv * inv;
+                cxs = fmaf(dx, w, cxs);
+                cys = fmaf(dy, w, cys);
+                czs = fmaf(dz, w, czs);
+            }
+            fx += cxs;
+            fy += cys;
+            fz += czs;
+            __syncwarp();
+        }
+        const NodeRec64 c = rec64[pr.y];
+        const float mx = (float)(c.cx - gx) - qx, my = (float)(c.cy - gy) - qy,
+                    mz = (float)(c.cz - gz) - qz;
+        const float inv = rsqrtf(fmaf(mx, mx, fmaf(my, my, fmaf(mz, mz, eps2))));
+        const float w = (float)(G * c.mass) * inv * inv * inv;
+        const float ex = fx - mx * w, ey = fy - my * w, ez = fz - mz * w;
+        float rel = valid ? sqrtf(ex * ex + ey * ey + ez * ez) / fmaxf(a_b, 1e-30f) : 0.f;
+        rel = warp_max(rel);
+        if (lane < NF) features[(size_t)q * NF + lane] = f[lane];
+        if (lane == 0) labels[q] = fminf(fmaxf(__log10f(fmaxf(rel, 1e-30f)), -12.f), 2.f) * 0.2f;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Training: FP32 forward / backward of the MLP (MSE loss), Adam
+// ---------------------------------------------------------------------------------------------
+constexpr int TR_BLOCK = 256;
+constexpr int TR_CHUNK = 64;
+
+__global__ void __launch_bounds__(TR_BLOCK)
+mlp_grad_kernel(const float* __restrict__ P, const float* __restrict__ X,
+                const float* __restrict__ Y, const uint32_t* __restrict__ idx, uint32_t n,
+                float* __restrict__ grad, float* __restrict__ loss) {
+    __shared__ float w[P_COUNT];
+    __shared__ float sx[TR_CHUNK][NF], sh1[TR_CHUNK][32], sh2[TR_CHUNK][32];
+    __shared__ float sd1[TR_CHUNK][32], sd2[TR_CHUNK][32], sdo[TR_CHUNK];
+    for (int k = threadIdx.x; k < P_COUNT; k += TR_BLOCK) w[k] = P[k];
+    float acc[6] = {0, 0, 0, 0, 0, 0};  // gradient entries threadIdx.x + i*TR_BLOCK
+    float lsum = 0;
+    const float inv_n = 1.0f / (float)n;
+    const uint32_t per_block = (n + gridDim.x - 1) / gridDim.x;
+    const uint32_t s0 = blockIdx.x * per_block, s1 = min(n, s0 + per_block);
+    __syncthreads();
+    for (uint32_t c0 = s0; c0 < s1; c0 += TR_CHUNK) {
+        const uint32_t cnt = min((uint32_t)TR_CHUNK, s1 - c0);
+        if (threadIdx.x < TR_CHUNK) {
+            const int s = threadIdx.x;
+            float xv[NF] = {0, 0, 0, 0, 0, 0, 0, 0}, h1[32], h2[32], d1[32], d2[32], dout = 0;
+            if ((uint32_t)s < cnt) {
+                const uint32_t row = idx ? idx[c0 + s] : c0 + s;
+                for (int i = 0; i < NF; ++i) xv[i] = X[(size_t)row * NF + i];
+                for (int o = 0; o < 32; ++o) {
+                    float a = w[P_B1 + o];
+                    for (int i = 0; i < NF; ++i) a = fmaf(xv[i], w[P_W1 + i * 32 + o], a);
+                    h1[o] = fmaxf(a, 0.f);
+                }
+                float out = w[P_B3];
+                for (int o = 0; o < 32; ++o) {
+                    float a = w[P_B2 + o];
+                    for (int i = 0; i < 32; ++i) a = fmaf(h1[i], w[P_W2 + i * 32 + o], a);
+                    h2[o] = fmaxf(a, 0.f);
+                    out = fmaf(h2[o], w[P_W3 + o], out);
+                }
+                const float e = out - Y[row];
+                lsum += e * e;
+                dout = 2.f * e * inv_n;
+                for (int o = 0; o < 32; ++o) d2[o] = h2[o] > 0.f ? dout * w[P_W3 + o] : 0.f;
+                for (int i = 0; i < 32; ++i) {
+                    float a = 0;
+                    for (int o = 0; o < 32; ++o) a = fmaf(d2[o], w[P_W2 + i * 32 + o], a);
+                    d1[i] = h1[i] > 0.f ? a : 0.f;
+                }
+            } else {
+                for (int o = 0; o < 32; ++o) h1[o] = h2[o] = d1[o] = d2[o] = 0.f;
+            }
+            for (int i = 0; i < NF; ++i) sx[s][i] = xv[i];
+            for (int o = 0; o < 32; ++o) {
+                sh1[s][o] = h1[o];
+                sh2[s][o] = h2[o];
+                sd1[s][o] = d1[o];
+                sd2[s][o] = d2[o];
+            }
+            sdo[s] = dout;
+        }
+        __syncthreads();
+        for (int i = 0; i < 6; ++i) {
+            const int e = threadIdx.x + i * TR_BLOCK;
+            if (e >= P_COUNT) break;
+            float a = 0;
+            if (e < P_B1) {  // W1[in][out]
+                const int in = e / 32, o = e % 32;
+                for (uint32_t s = 0; s < cnt; ++s) a = fmaf(sx[s][in], sd1[s][o], a);
+            } else if (e < P_W2) {
+                const int o = e - P_B1;
+                for (uint32_t s = 0; s < cnt; ++s) a += sd1[s][o];
+            } else if (e < P_B2) {
+                const int in = (e - P_W2) / 32, o = (e - P_W2) % 32;
+                for (uint32_t s = 0; s < cnt; ++s) a = fmaf(sh1[s][in], sd2[s][o], a);
+            } else if (e < P_W3) {
+                const int o = e - P_B2;
+                for (uint32_t s = 0; s < cnt; ++s) a += sd2[s][o];
+            } else if (e < P_B3) {
+                const int in = e - P_W3;
+                for (uint32_t s = 0; s < cnt; ++s) a = fmaf(sh2[s][in], sdo[s], a);
+            } else {
+                for (uint32_t s = 0; s < cnt; ++s) a += sdo[s];
+            }
+            acc[i] += a;
+        }
+        __syncthreads();
+    }
+    for (int i = 0; i < 6; ++i) {
+        const int e = threadIdx.x + i * TR_BLOCK;
+        if (e < P_COUNT) atomicAdd(&grad[e], acc[i]);
+    }
+    if (threadIdx.x < TR_CHUNK) atomicAdd(loss, lsum * inv_n);
+}
+
+__global__ void mlp_adam_kernel(float* __restrict__ P, float* __restrict__ M, float* __restrict__ V,
+                                const float* __restrict__ grad, float lr, float b1, float b2,
+                                float eps, float c1, float c2) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P_COUNT) return;
+    const float g = grad[k];
+    const float m = b1 * M[k] + (1.f - b1) * g;
+    const float v = b2 * V[k] + (1.f - b2) * g * g;
+    M[k] = m;
+    V[k] = v;
+    P[k] -= lr * (m * c1) / (sqrtf(v * c2) + eps);
+}
+
+__global__ void mlp_predict_kernel(const float* __restrict__ P, const float* __restrict__ X,
+                                   uint32_t n, float* __restrict__ out) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    float xv[NF], h1[32];
+    for (int i = 0; i < NF; ++i) xv[i] = X[(size_t)s * NF + i];
+    for (int o = 0; o < 32; ++o) {
+        float a = P[P_B1 + o];
+        for (int i = 0; i < NF; ++i) a = fmaf(xv[i], P[P_W1 + i * 32 + o], a);
+        h1[o] = fmaxf(a, 0.f);
+    }
+    float res = P[P_B3];
+    for (int o = 0; o < 32; ++o) {
+        float a = P[P_B2 + o];
+        for (int i = 0; i < 32; ++i) a = fmaf(h1[i], P[P_W2 + i * 32 + o], a);
+        res = fmaf(fmaxf(a, 0.f), P[P_W3 + o], res);
+    }
+    out[s] = res;
+}
+
+// BF16 tensor-core inference of the same network (16 rows per warp), for validating mlp16.
+__global__ void __launch_bounds__(128)
+mlp_predict_bf16_kernel(const float* __restrict__ P, const float* __restrict__ X, uint32_t n,
+                        float* __restrict__ out) {
+    __shared__ __align__(16) __nv_bfloat16 feat[4][16][16];
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    MlpFrags F;
+    load_frags(P, lane, F);
+    __nv_bfloat16* fm = &feat[wi][0][0];
+    for (uint32_t base = (blockIdx.x * 4 + wi) * 16; base < n; base += gridDim.x * 4 * 16) {
+        for (int k = lane; k < 256; k += 32) {
+            const uint32_t r = base + k / 16;
+            const int c = k % 16;
+            fm[k] = __float2bfloat16(c < NF && r < n ? X[(size_t)r * NF + c] : 0.f);
+        }
+        __syncwarp();
+        const float s = mlp16(fm, lane, F);
+        if (lane < 16 && base + lane < n) out[base + lane] = s;
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+nb_status nb_mlp_param_count(uint32_t* out) {
+    if (!out) return nb::set_error(NB_ERR_INVALID_ARG, "null output");
+    *out = P_COUNT;
+    return NB_OK;
+}
+
+nb_status nb_mlp_loss_grad(nb_ctx* ctx, const float* params, const float* X, const float* Y,
+                           const uint32_t* idx, uint32_t n, float* grad, float* loss,
+                           nb_stream_t stream) {
+    NB_CHECK_CTX(ctx);
+    if (!params || !X || !Y || !grad || !loss || n == 0)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_mlp_loss_grad: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    NB_CUDA_TRY(cudaMemsetAsync(grad, 0, P_COUNT * sizeof(float), s));
+    NB_CUDA_TRY(cudaMemsetAsync(loss, 0, sizeof(float), s));
+    int blocks = nb::ceil_div(n, TR_CHUNK * 4);
+    if (blocks > ctx->sm_count * 2) blocks = ctx->sm_count * 2;
+    mlp_grad_kernel<<<blocks, TR_BLOCK, 0, s>>>(params, X, Y, idx, n, grad, loss);
+    return nb::check_launch("mlp_grad_kernel");
+}
+
+nb_status nb_mlp_adam(nb_ctx* ctx, float* params, float* m, float* v, const float* grad,
+                      float lr, float beta1, float beta2, float eps, int step,
+                      nb_stream_t stream) {
+    NB_CHECK_CTX(ctx);
+    if (!params || !m || !v || !grad || step < 1)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_mlp_adam: bad arguments");
+    const float c1 = 1.f / (1.f - powf(beta1, (float)step));
+    const float c2 = 1.f / (1.f - powf(beta2, (float)step));
+    mlp_adam_kernel<<<nb::ceil_div(P_COUNT, 256), 256, 0, (cudaStream_t)stream>>>(
+        params, m, v, grad, lr, beta1, beta2, eps, c1, c2);
+    return nb::check_launch("mlp_adam_kernel");
+}
+
+nb_status nb_mlp_predict(nb_ctx* ctx, const float* params, const float* X, uint32_t n,
+                         float* out, int bf16_tensor_cores, nb_stream_t stream) {
+    NB_CHECK_CTX(ctx);
+    if (!params || !X || !out) return nb::set_error(NB_ERR_INVALID_ARG, "nb_mlp_predict: null");
+    if (n == 0) return NB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (bf16_tensor_cores) {
+        int blocks = nb::ceil_div(n, 64);
+        if (blocks > ctx->sm_count * 8) blocks = ctx->sm_count * 8;
+        mlp_predict_bf16_kernel<<<blocks, 128, 0, s>>>(params, X, n, out);
+        return nb::check_launch("mlp_predict_bf16_kernel");
+    }
+    mlp_predict_kernel<<<nb::ceil_div(n, 128), 128, 0, s>>>(params, X, n, out);
+    return nb::check_launch("mlp_predict_kernel");
+}
+
+nb_status nb_bh_set_policy(nb_bh_tree* t, const float* params_dev, float log10_tau,
+                           double theta_fallback, uint32_t count_cap) {
+    if (!t) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_set_policy: null tree");
+    t->policy = params_dev;
+    t->policy_log_tau = log10_tau;
+    t->policy_theta = (float)theta_fallback;
+    t->policy_count_cap = count_cap;
+    return NB_OK;
+}
+
+nb_status nb_bh_generate_pairs(nb_ctx* ctx, const nb_bh_tree* t, const double* m,
+                               const double* x, const double* y, const double* z,
+                               const double* ax, const double* ay, const double* az, double G,
+                               double eps2, double theta_gen, double sample_fraction,
+                               uint32_t seed, uint32_t count_cap, uint32_t max_pairs,
+                               float* features, float* labels, uint32_t* count_dev,
+                               uint32_t* pairs_out, nb_stream_t stream) {
+    NB_CHECK_CTX(ctx);
+    if (!t || !t->built) return nb::set_error(NB_ERR_NOT_BUILT, "nb_bh_generate_pairs: tree not built");
+    if (!m || !x || !y || !z || !ax || !ay || !az || !features || !labels || !count_dev ||
+        max_pairs == 0 || !(sample_fraction > 0) || sample_fraction > 1)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_generate_pairs: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    void* buf = nullptr;
+    NB_TRY(nb::scratch(ctx, NB_SCRATCH_LABELS, (size_t)max_pairs * sizeof(uint2), &buf));
+    NB_CUDA_TRY(cudaMemsetAsync(count_dev, 0, sizeof(uint32_t), s));
+    const uint32_t warps = (t->n + 31) / 32;
+    const uint32_t threshold = (uint32_t)(sample_fraction * 4294967295.0);
+    pairs_collect_kernel<<<nb::ceil_div((long long)warps * 32, 128), 128, 0, s>>>(
+        t->rec32, t->aux, t->info, t->ids, x, y, z, ax, ay, az, t->box, t->n,
+        (float)(theta_gen * theta_gen), count_cap, threshold, seed, (uint2*)buf, max_pairs,
+        (unsigned int*)count_dev);
+    NB_TRY(nb::check_launch("pairs_collect_kernel"));
+    pairs_label_kernel<<<ctx->sm_count * 8, 128, 0, s>>>(
+        t->rec32, t->rec64, t->aux, t->ids, m, x, y, z, ax, ay, az, t->box, t->n, G, (float)eps2,
+        count_cap, (const uint2*)buf, (const unsigned int*)count_dev, max_pairs, features, labels);
+    NB_TRY(nb::check_launch("pairs_label_kernel"));
+    if (pairs_out)
+        NB_CUDA_TRY(cudaMemcpyAsync(pairs_out, buf, (size_t)max_pairs * sizeof(uint2),
+                                    cudaMemcpyDeviceToDevice, s));
+    return NB_OK;
+}
+
+}  // extern "C"
+
+namespace nb {
+
+nb_status launch_learned(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const double* y,
+                         const double* z, double* ax, double* ay, double* az, double eps2,
+                         unsigned long long* counters, cudaStream_t s) {
+    if (!t->policy)
+        return set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: NB_OPEN_LEARNED needs nb_bh_set_policy");
+    const uint32_t warps = (t->n + 31) / 32;
+    bh_learned_kernel<<<ceil_div(warps, LT_WARPS), LT_THREADS, 0, s>>>(
+        t->rec32, t->aux, t->children, t->sorted4, t->info, t->ids, x, y, z, t->box, t->n, t->policy,
+        t->policy_log_tau * 0.2f, t->policy_theta * t->policy_theta, t->policy_count_cap,
+        (float)eps2, ax, ay, az, counters, ctx->dev_error);
+    return check_launch("bh_learned_kernel");
+}
+
+}  // namespace nb

@@ -91,6 +91,50 @@ naive_f64_kernel(const double* __restrict__ m, const double* __restrict__ x,
     }
 }
 
+// FP64 accelerations of listed target bodies (ax[t] for targets[t]); FMAs + refined rsqrt.
+__global__ void __launch_bounds__(F64_THREADS)
+naive_f64_targets_kernel(const double* __restrict__ m, const double* __restrict__ x,
+                         const double* __restrict__ y, const double* __restrict__ z, uint32_t n,
+                         const uint32_t* __restrict__ targets, uint32_t n_t,
+                         double* __restrict__ ax, double* __restrict__ ay,
+                         double* __restrict__ az, double G, double eps2) {
+    __shared__ double sx[F64_THREADS], sy[F64_THREADS], sz[F64_THREADS], sm[F64_THREADS];
+    const uint32_t t = blockIdx.x * F64_THREADS + threadIdx.x;
+    const bool active = t < n_t;
+    const uint32_t i = active ? targets[t] : 0;
+    const double px = active ? x[i] : 0, py = active ? y[i] : 0, pz = active ? z[i] : 0;
+    double acc_x = 0, acc_y = 0, acc_z = 0;
+    for (uint32_t k = 0; k < n; k += F64_THREADS) {
+        const uint32_t j = k + threadIdx.x;
+        if (j < n) {
+            sx[threadIdx.x] = x[j];
+            sy[threadIdx.x] = y[j];
+            sz[threadIdx.x] = z[j];
+            sm[threadIdx.x] = m[j];
+        }
+        __syncthreads();
+        const uint32_t cnt = min((uint32_t)F64_THREADS, n - k);
+        if (active) {
+#pragma unroll 4
+            for (uint32_t jj = 0; jj < cnt; ++jj) {
+                const double r_x = sx[jj] - px, r_y = sy[jj] - py, r_z = sz[jj] - pz;
+                double den = fma(r_x, r_x, fma(r_y, r_y, fma(r_z, r_z, eps2)));
+                den = den * den * den;
+                const double s = sm[jj] * nb_rsqrt_f64(den);
+                acc_x = fma(s, r_x, acc_x);
+                acc_y = fma(s, r_y, acc_y);
+                acc_z = fma(s, r_z, acc_z);
+            }
+        }
+        __syncthreads();
+    }
+    if (active) {
+        ax[t] = acc_x * G;
+        ay[t] = acc_y * G;
+        az[t] = acc_z * G;
+    }
+}
+
 // ---------------------------------------------------------------------------------------------
 // FP32, compensated: the batched pair kernel (nb_pair.cuh) with a batch of one system whose
 // targets are [i_begin, i_end).
@@ -183,6 +227,20 @@ nb_status nb_naive_accel(nb_ctx* ctx, const double* m, const double* x, const do
         return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_accel: block_size must be >= 0");
     return naive_dispatch(ctx, m, x, y, z, ax, ay, az, n, 0, n, G, eps2, prec,
                           (cudaStream_t)stream);
+}
+
+nb_status nb_naive_accel_targets(nb_ctx* ctx, const double* m, const double* x, const double* y,
+                                 const double* z, uint32_t n, const uint32_t* targets,
+                                 uint32_t n_targets, double* ax, double* ay, double* az, double G,
+                                 double eps2, nb_stream_t stream) {
+    NB_CHECK_CTX(ctx);
+    if (!m || !x || !y || !z || !targets || !ax || !ay || !az)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_accel_targets: null pointer");
+    if (n == 0 || n_targets == 0) return NB_OK;
+    naive_f64_targets_kernel<<<nb::ceil_div(n_targets, F64_THREADS), F64_THREADS, 0,
+                               (cudaStream_t)stream>>>(m, x, y, z, n, targets, n_targets, ax, ay,
+                                                       az, G, eps2);
+    return nb::check_launch("naive_f64_targets_kernel");
 }
 
 nb_status nb_naive_set_pair_config(int config) {

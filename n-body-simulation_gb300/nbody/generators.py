@@ -132,3 +132,28 @@ def write_csv(path: str, bodies: dict):
         for i in range(len(bodies["m"])):
             vals = ",".join(repr(float(c[i])) for c in cols)
             f.write(f"{i},{bodies['names'][i]},{bodies['classes'][i]},{vals}\n")
+
+
+def disc_plummer_mix(n: int, seed: int = 1, plummer_mass_msun: float = 1e-3,
+                     plummer_radius_au: float = 0.05, plummer_distance_au: float = 5.0):
+    """Half heliocentric disc, half Plummer sphere (total mass 1e-3 Msun, scale radius 0.05 AU)
+    centred 5 AU from the central body on a circular heliocentric orbit (bulk velocity along +y),
+    with internal velocities from the Plummer distribution function. Masses in kg."""
+    n_disc = n // 2
+    d = heliocentric_disc(n_disc, seed)
+    pl = plummer(n - n_disc, seed + 1000003)
+    G = d["G"]
+    m_pl = plummer_mass_msun * MSUN_KG
+    a = plummer_radius_au
+    vscale = np.sqrt(G * m_pl / a)  # Henon velocity unit for (G, M, a)
+    vc = np.sqrt(G * MSUN_KG / plummer_distance_au)
+    out = {"m": np.concatenate([d["m"], pl["m"] * m_pl]),
+           "x": np.concatenate([d["x"], pl["x"] * a + plummer_distance_au]),
+           "y": np.concatenate([d["y"], pl["y"] * a]),
+           "z": np.concatenate([d["z"], pl["z"] * a]),
+           "vx": np.concatenate([d["vx"], pl["vx"] * vscale]),
+           "vy": np.concatenate([d["vy"], pl["vy"] * vscale + vc]),
+           "vz": np.concatenate([d["vz"], pl["vz"] * vscale]),
+           "names": d["names"] + [f"cluster{k}" for k in range(n - n_disc)],
+           "classes": d["classes"] + ["AST"] * (n - n_disc), "G": G}
+    return out

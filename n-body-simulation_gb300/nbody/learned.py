@@ -1,0 +1,137 @@
+"""Training and evaluation of the learned opening policy (driver code over the C ABI).
+
+Pipeline (all compute in libnbody_cuda.so kernels):
+  1. labelled pairs: for seeded systems, FP32-naive reference accelerations, a tree build, and
+     nb_bh_generate_pairs (a theta-rule walk samples (32-body group, cell) pairs; each gets 8
+     features and the label log10(worst relative error of the cell's monopole)/5);
+  2. training: Adam on the mean-squared error with nb_mlp_loss_grad / nb_mlp_adam;
+  3. evaluation: force errors of a traversal against FP64 naive accelerations of sampled bodies
+     (nb_naive_accel_targets), and a sweep of the acceptance threshold (or of theta for the
+     group rule) to compare both at matched error.
+"""
+
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+from . import generators
+from .lib import BHTree, Context, MLP_PARAMS, mlp_adam, mlp_loss_grad
+
+EPS2 = 1e-22
+
+
+def _dev(a, dtype=None):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(a), device="cuda", dtype=dtype)
+
+
+def reference_accelerations(ctx: Context, t: dict, G: float):
+    """FP32-compensated naive accelerations (|a| reference for labels and the first step)."""
+    import torch
+    n = t["m"].numel()
+    a = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, G, EPS2, "f32c")
+    return a
+
+
+def make_pairs(ctx: Context, d: dict, max_pairs: int, theta_gen: float = 0.3, seed: int = 0,
+               count_cap: int = 8192):
+    """Labelled (features, labels) pairs of one system on the device."""
+    t = {k: _dev(d[k]) for k in ("m", "x", "y", "z")}
+    n = t["m"].numel()
+    a = reference_accelerations(ctx, t, d["G"])
+    tree = BHTree(ctx, n, theta=0.5)
+    tree.build(t["m"], t["x"], t["y"], t["z"], d["G"])
+    # count candidates with a tiny buffer, then sample the wanted number
+    _, _, _, found = tree.generate_pairs(t["m"], t["x"], t["y"], t["z"], *a, d["G"], EPS2,
+                                         theta_gen, 1.0, seed, count_cap, 1)
+    frac = min(1.0, max_pairs / max(found, 1))
+    X, Y, _, _ = tree.generate_pairs(t["m"], t["x"], t["y"], t["z"], *a, d["G"], EPS2, theta_gen,
+                                     frac, seed, count_cap, max_pairs)
+    ctx.sync()
+    tree.close()
+    return X.clone(), Y.clone(), found
+
+
+def init_params(seed: int = 0):
+    rng = np.random.default_rng(seed)
+    p = []
+    for fan_in, fan_out in ((8, 32), (32, 32)):
+        lim = math.sqrt(6.0 / (fan_in + fan_out))
+        p.append(rng.uniform(-lim, lim, size=(fan_in, fan_out)).ravel())
+        p.append(np.zeros(fan_out))
+    lim = math.sqrt(6.0 / 33)
+    p.append(rng.uniform(-lim, lim, size=32))
+    p.append(np.array([-1.0]))
+    return np.concatenate(p).astype(np.float32)
+
+
+def train(ctx: Context, X, Y, epochs: int = 4, batch: int = 8192, lr: float = 2e-3, seed: int = 0,
+          log=None):
+    """Adam on the device; returns (params [1377] float32 cuda tensor, per-epoch mean losses)."""
+    import torch
+    n = X.shape[0]
+    params = _dev(init_params(seed))
+    m = torch.zeros(MLP_PARAMS, dtype=torch.float32, device="cuda")
+    v = torch.zeros_like(m)
+    grad = torch.zeros_like(m)
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    step = 0
+    history = []
+    for ep in range(epochs):
+        perm = torch.randperm(n, device="cuda", generator=gen).to(torch.int32)
+        tot = torch.zeros(1, dtype=torch.float32, device="cuda")
+        nb = 0
+        for b0 in range(0, n, batch):
+            idx = perm[b0:b0 + batch]
+            mlp_loss_grad(ctx, params, X, Y, idx, idx.numel(), grad, loss)
+            step += 1
+            lr_t = lr * (0.5 * (1 + math.cos(math.pi * step / (epochs * math.ceil(n / batch)))))
+            mlp_adam(ctx, params, m, v, grad, max(lr_t, lr * 0.02), 0.9, 0.999, 1e-8, step)
+            tot += loss
+            nb += 1
+        history.append(float(tot.item()) / nb)
+        if log:
+            log(f"epoch {ep}: mse {history[-1]:.5f}")
+    return params, history
+
+
+def sample_targets(n: int, k: int, seed: int = 7):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, size=min(k, n), replace=False)).astype(np.uint32)
+
+
+def fp64_reference(ctx: Context, t: dict, G: float, targets):
+    import torch
+    tg = _dev(targets.view(np.int32))
+    k = len(targets)
+    a = [torch.zeros(k, dtype=torch.float64, device="cuda") for _ in range(3)]
+    ctx.naive_accel_targets(t["m"], t["x"], t["y"], t["z"], tg, *a, G, EPS2)
+    ctx.sync()
+    return [v.cpu().numpy() for v in a]
+
+
+def errors(acc, ref, targets):
+    ax, ay, az = (a.cpu().numpy()[targets] for a in acc)
+    rx, ry, rz = ref
+    num = np.sqrt((ax - rx) ** 2 + (ay - ry) ** 2 + (az - rz) ** 2)
+    e = num / np.sqrt(rx * rx + ry * ry + rz * rz)
+    return float(np.median(e)), float(np.percentile(e, 99))
+
+
+def timed(fn, reps=3):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps

@@ -150,6 +150,11 @@ class Context:
         check(self.lib.nb_energy(self.handle, ptr(m), ptr(x), ptr(y), ptr(z), ptr(vx), ptr(vy),
                                  ptr(vz), m.numel(), G, ptr(out), stream_ptr(stream)))
 
+    def naive_accel_targets(self, m, x, y, z, targets, ax, ay, az, G, eps2, stream=None):
+        check(self.lib.nb_naive_accel_targets(self.handle, ptr(m), ptr(x), ptr(y), ptr(z),
+                                              m.numel(), ptr(targets), targets.numel(), ptr(ax),
+                                              ptr(ay), ptr(az), G, eps2, stream_ptr(stream)))
+
     def aabb(self, x, y, z, out, stream=None):
         check(self.lib.nb_aabb(self.handle, ptr(x), ptr(y), ptr(z), x.numel(), ptr(out),
                                stream_ptr(stream)))
@@ -206,6 +211,16 @@ SIGNATURES.update({
     "nb_batch_graph_create": [_vp, _vp] + [_vp] * 13 + [_d, _d, _d, _i, C.POINTER(_vp)],
     "nb_graph_launch": [_vp, _vp],
     "nb_graph_destroy": [_vp],
+    "nb_mlp_param_count": [C.POINTER(_u32)],
+    "nb_mlp_loss_grad": [_vp] + [_vp] * 4 + [_u32, _vp, _vp, _vp],
+    "nb_mlp_adam": [_vp] + [_vp] * 4 + [C.c_float] * 4 + [_i, _vp],
+    "nb_mlp_predict": [_vp, _vp, _vp, _u32, _vp, _i, _vp],
+    "nb_bh_generate_pairs": [_vp, _vp] + [_vp] * 7 + [_d, _d, _d, _d, _u32, _u32, _u32, _vp, _vp,
+                                                     _vp, _vp, _vp],
+    "nb_bh_export_node_ranges": [_vp, _vp, _vp, _vp, _vp],
+    "nb_naive_accel_targets": [_vp] + [_vp] * 4 + [_u32, _vp, _u32] + [_vp] * 3 + [_d, _d, _vp],
+    "nb_bh_set_policy": [_vp, _vp, C.c_float, _d, _u32],
+    "nb_bh_accel_learned_counted": [_vp, _vp] + [_vp] * 6 + [_d, _vp, _vp],
 })
 
 
@@ -267,6 +282,46 @@ class BHTree:
         self.ctx.sync(stream)
         a, o = out.cpu().tolist()
         return int(a), int(o)
+
+    def export_node_ranges(self):
+        import numpy as np
+        nc = self.stats()["node_count"]
+        a = [np.zeros(nc, dtype=np.uint32) for _ in range(4)]
+        check(self.lib.nb_bh_export_node_ranges(self.handle, *[v.ctypes.data for v in a]))
+        return {"first": a[0], "count": a[1], "level": a[2], "body": a[3]}
+
+    def set_policy(self, params, log10_tau, theta_fallback=0.5, count_cap=8192):
+        self._policy = params  # keep the device tensor alive
+        check(self.lib.nb_bh_set_policy(self.handle, ptr(params), log10_tau, theta_fallback,
+                                        count_cap))
+
+    def accel_learned_counted(self, x, y, z, ax, ay, az, eps2, stream=None):
+        import torch
+        cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        check(self.lib.nb_bh_accel_learned_counted(self.ctx.handle, self.handle, ptr(x), ptr(y),
+                                                   ptr(z), ptr(ax), ptr(ay), ptr(az), eps2,
+                                                   ptr(cnt), stream_ptr(stream)))
+        self.ctx.sync(stream)
+        a, b = cnt.cpu().tolist()
+        return int(a), int(b)
+
+    def generate_pairs(self, m, x, y, z, ax, ay, az, G, eps2, theta_gen, sample_fraction, seed,
+                       count_cap, max_pairs, with_ids=False, stream=None):
+        """(features [k,8], labels [k], pair ids [k,2] or None, pairs found) on the device."""
+        import torch
+        f = torch.empty((max_pairs, 8), dtype=torch.float32, device="cuda")
+        lab = torch.empty(max_pairs, dtype=torch.float32, device="cuda")
+        cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+        ids = torch.empty((max_pairs, 2), dtype=torch.int32, device="cuda") if with_ids else None
+        check(self.lib.nb_bh_generate_pairs(self.ctx.handle, self.handle, ptr(m), ptr(x), ptr(y),
+                                            ptr(z), ptr(ax), ptr(ay), ptr(az), G, eps2, theta_gen,
+                                            sample_fraction, seed, count_cap, max_pairs, ptr(f),
+                                            ptr(lab), ptr(cnt), ptr(ids) if with_ids else None,
+                                            stream_ptr(stream)))
+        self.ctx.sync(stream)
+        found = int(cnt.item())
+        k = min(found, max_pairs)
+        return f[:k], lab[:k], (ids[:k] if with_ids else None), found
 
     def export_order(self, n):
         import numpy as np
@@ -396,3 +451,21 @@ class Graph:
             self.close()
         except Exception:
             pass
+
+
+MLP_PARAMS = 1377
+
+
+def mlp_loss_grad(ctx, params, X, Y, idx, n, grad, loss, stream=None):
+    check(load().nb_mlp_loss_grad(ctx.handle, ptr(params), ptr(X), ptr(Y), ptr(idx), n, ptr(grad),
+                                  ptr(loss), stream_ptr(stream)))
+
+
+def mlp_adam(ctx, params, m, v, grad, lr, beta1, beta2, eps, step, stream=None):
+    check(load().nb_mlp_adam(ctx.handle, ptr(params), ptr(m), ptr(v), ptr(grad), lr, beta1, beta2,
+                             eps, step, stream_ptr(stream)))
+
+
+def mlp_predict(ctx, params, X, out, bf16=False, stream=None):
+    check(load().nb_mlp_predict(ctx.handle, ptr(params), ptr(X), X.shape[0], ptr(out),
+                                1 if bf16 else 0, stream_ptr(stream)))
