@@ -96,7 +96,7 @@ nb_status nb_naive_accel_targets(nb_ctx* ctx, const double* m, const double* x, 
 nb_status nb_naive_set_pair_config(int config);
 
 /* ---------------------------------------------------------------------------------------------
- * Batched ensembles (the spec batching form; the reference simulates one system).
+ * Batched ensembles (the batching form of the method; the reference simulates one system).
  * Many independent systems of uneven size in concatenated FP64 arrays (system s owns bodies
  * [sum(counts[0..s)), +counts[s])). Forces use FP32 pair math with compensated accumulation, one
  * persistent stream-K launch for all systems; integration stays FP64 (nb_leapfrog_* over all
@@ -292,7 +292,7 @@ nb_status nb_bh_count_interactions(nb_ctx* ctx, const nb_bh_tree* tree, const do
 nb_status nb_util_fma_peak(nb_ctx* ctx, int fp64, double* flops_per_s);
 
 /* ---------------------------------------------------------------------------------------------
- * Learned opening policy (the spec learned form; no reference counterpart).
+ * Learned opening policy (the learned form of the method; no reference counterpart).
  * Network: 8 features -> 32 -> 32 -> 1 (ReLU), NB_MLP_PARAMS FP32 parameters in the layout
  * W1[8][32], b1[32], W2[32][32], b2[32], w3[32], b3 (all DEVICE arrays). It predicts
  * y = log10(worst relative force error of accepting a cell for a 32-body group) / 5.
@@ -328,11 +328,14 @@ nb_status nb_bh_generate_pairs(nb_ctx* ctx, const nb_bh_tree* tree, const double
                                uint32_t* pairs_out, nb_stream_t stream);
 /* Policy of NB_OPEN_LEARNED: accept a cell when the network predicts an error below tau;
  * cells with more than count_cap bodies use the group theta rule with theta_fallback. The
- * traversal reads |a| of the previous step from the ax, ay, az arrays it then overwrites. */
+ * traversal reads |a| of the previous step from the ax, ay, az arrays it then overwrites.
+ * params_dev NULL selects the same walk with the group theta rule (theta_fallback) in place of
+ * the network: the method without it. */
 nb_status nb_bh_set_policy(nb_bh_tree* tree, const float* params_dev, float log10_tau,
                            double theta_fallback, uint32_t count_cap);
-/* NB_OPEN_LEARNED traversal that also counts body-cell interactions (counters_dev[0]) and
- * network evaluations (counters_dev[1]) into 2 DEVICE uint64. */
+/* NB_OPEN_LEARNED traversal that also counts, into 4 DEVICE uint64: body-cell interactions
+ * (counters_dev[0]), cells decided by the policy (network, or theta rule when the policy has no
+ * network) ([1]), cells visited ([2]) and walk steps of up to 32 cells ([3]), summed over groups. */
 nb_status nb_bh_accel_learned_counted(nb_ctx* ctx, const nb_bh_tree* tree, const double* x,
                                       const double* y, const double* z, double* ax, double* ay,
                                       double* az, double eps2, unsigned long long* counters_dev,

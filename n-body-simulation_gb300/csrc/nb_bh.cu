@@ -254,6 +254,7 @@ struct ComArgs {
     const uint32_t* node_first_pos;
     uint32_t* children;
     float4* sorted4;
+    float4* sorted4lo;
 };
 
 __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double cy, double cz,
@@ -319,7 +320,10 @@ __global__ void com_kernel(ComArgs A) {
     A.mass[idx] = mb;
     A.q[idx] = qb;
     A.node_count[idx] = 1;
-    A.sorted4[p] = make_float4((float)rx, (float)ry, (float)rz, (float)(A.G * mb));
+    const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
+    A.sorted4[p] = make_float4(hx, hy, hz, (float)(A.G * mb));
+    A.sorted4lo[p] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy),
+                                 (float)(rz - (double)hz), 0.f);
     write_records(A, idx, cx, cy, cz, mb, qb, 1, A.node_level[idx], A.node_skip[idx], b);
     uint32_t cur = A.node_parent[idx];
     while (cur != NB_NONE) {
@@ -419,6 +423,7 @@ void carve(nb_bh_tree* t, Carver& c) {
     t->aux = c.take<NodeAux>(cap);
     t->children = c.take<uint32_t>(cap * 8);
     t->sorted4 = c.take<float4>(n);
+    t->sorted4lo = c.take<float4>(n);
 }
 
 }  // namespace
@@ -555,6 +560,7 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     A.node_first_pos = t->node_first;
     A.children = t->children;
     A.sorted4 = t->sorted4;
+    A.sorted4lo = t->sorted4lo;
     com_kernel<<<grid, BH_THREADS, 0, s>>>(A);
     NB_TRY(nb::check_launch("com_kernel"));
     t->built = true;

@@ -68,8 +68,10 @@ struct nb_bh_tree {
     NodeAux* aux = nullptr;
     uint32_t* children = nullptr;  // 8 per node: children in visit order, NB_NONE padded
     float4* sorted4 = nullptr;     // per sorted position: position relative to the box centre, G*m
+    float4* sorted4lo = nullptr;   // per sorted position: FP32 residual of that position (x, y, z)
     // learned opening policy (device parameters, see nb_learned.cu)
-    const float* policy = nullptr;
+    const float* policy = nullptr;  // nullptr after nb_bh_set_policy: theta rule, same walk
+    bool policy_set = false;
     float policy_log_tau = 0.f;
     float policy_theta = 0.5f;
     uint32_t policy_count_cap = 8192;

@@ -29,7 +29,7 @@ constexpr int NF = 8;
 constexpr float SQRT3 = 1.7320508f;
 
 struct GroupGeo {
-    float cx, cy, cz, r, a_ref;
+    float cx, cy, cz, r, a_ref, lg_aref;  // lg_aref = log2(a_ref)
     float hx, hy, hz;  // half extents of the group's bounding box
 };
 
@@ -59,13 +59,16 @@ __device__ GroupGeo group_geo(bool valid, float px, float py, float pz, float a_
     const float dx = px - g.cx, dy = py - g.cy, dz = pz - g.cz;
     g.r = warp_max(valid ? sqrtf(dx * dx + dy * dy + dz * dz) : 0.f);
     g.a_ref = fmaxf(warp_min(valid ? a_prev : inf), 1e-30f);
+    g.lg_aref = __log2f(g.a_ref);
     return g;
 }
 
 // The 8 features of a (group, cell) pair and the cell's class: 0 = decide with the network,
 // 1 = body leaf (accept), 2 = may overlap the group (open), 3 = outside the training range
 // (theta rule). gap = the smallest distance from a member of the group to the cell's centre of
-// mass; d = distance from the group's box centre.
+// mass; d = distance from the group's box centre. Ratios use the fast reciprocal and logarithms
+// the fast base-2 logarithm (features only steer the policy; labels and training use the same
+// function).
 __device__ __forceinline__ int cell_features(const NodeRec32& r, const NodeAux& x,
                                              const GroupGeo& g, float gap, uint32_t count_cap,
                                              float* f) {
@@ -74,15 +77,19 @@ __device__ __forceinline__ int cell_features(const NodeRec32& r, const NodeAux& 
     if (gap <= SQRT3 * e) return 2;
     if (x.count > count_cap) return 3;
     const float dx = r.cx - g.cx, dy = r.cy - g.cy, dz = r.cz - g.cz;
-    const float d = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-    f[0] = __log2f(d / e) * 0.25f;
-    f[1] = x.spread / e;
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float inv_d = rsqrtf(d2);
+    const float lg_e = __log2f(e), lg_gap = __log2f(gap);
+    const float lg_d = 0.5f * __log2f(d2);
+    f[0] = (lg_d - lg_e) * 0.25f;
+    f[1] = __fdividef(x.spread, e);
     f[2] = __log2f((float)x.count) * 0.0625f;
     f[3] = (float)r.level * 0.0625f;
-    f[4] = g.r / d;
-    f[5] = __log10f(fmaxf(r.gm, 1e-37f) / (gap * gap * g.a_ref)) * 0.25f;
-    f[6] = __log2f(gap / e) * 0.25f;
-    f[7] = x.spread / gap;
+    f[4] = g.r * inv_d;
+    // log10(G m / (gap^2 a_ref)) / 4
+    f[5] = (__log2f(fmaxf(r.gm, 1e-37f)) - 2.f * lg_gap - g.lg_aref) * (0.30103f * 0.25f);
+    f[6] = (lg_gap - lg_e) * 0.25f;
+    f[7] = __fdividef(x.spread, gap);
     return 0;
 }
 
@@ -111,54 +118,65 @@ __device__ __forceinline__ void mma16816(float* c, uint32_t a0, uint32_t a1, uin
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// Weight fragments of one lane (g = lane/4, t = lane%4).
-struct MlpFrags {
-    uint32_t w1[4];        // layer 1, n-tile nt: W1[2t..2t+1][nt*8+g] (k rows 8..15 are zero)
-    uint32_t w2[2][4][2];  // layer 2, k-step ks, n-tile nt
-    uint32_t w3[2][2];     // layer 3 (output column 0 only: lanes with g == 0)
-    float b1[4][2], b2[4][2], b3;
+// Weight fragments of one lane (g = lane/4, t = lane%4), flat:
+//  w[nt]                      layer 1, n-tile nt: W1[2t..2t+1][nt*8+g] (k rows 8..15 are zero)
+//  w[4 + (ks*4 + nt)*2 + j]   layer 2, k-step ks, n-tile nt, register j
+//  w[20 + ks*2 + j]           layer 3 (output column 0 only: lanes with g == 0)
+//  b[nt*2 + j], b[8 + nt*2 + j], b[16]: biases of layers 1, 2 and 3 for the lane's columns.
+// They live in shared memory, [index][lane] (conflict-free), shared by the block's warps.
+constexpr int MF_W = 24, MF_B = 17;
+struct MlpFragsSmem {
+    const uint32_t* ws;
+    const float* bs;
+    int lane;
+    __device__ __forceinline__ uint32_t w(int i) const { return ws[i * 32 + lane]; }
+    __device__ __forceinline__ float b(int i) const { return bs[i * 32 + lane]; }
 };
 
-__device__ void load_frags(const float* __restrict__ P, int lane, MlpFrags& F) {
+__device__ void load_frags(const float* __restrict__ P, int lane, uint32_t* w, float* b,
+                           int stride) {
     const int g = lane >> 2, t = lane & 3;
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt) {
         const int o = nt * 8 + g;
-        F.w1[nt] = pack_bf16(P[P_W1 + (2 * t) * 32 + o], P[P_W1 + (2 * t + 1) * 32 + o]);
-        F.b1[nt][0] = P[P_B1 + nt * 8 + 2 * t];
-        F.b1[nt][1] = P[P_B1 + nt * 8 + 2 * t + 1];
-        F.b2[nt][0] = P[P_B2 + nt * 8 + 2 * t];
-        F.b2[nt][1] = P[P_B2 + nt * 8 + 2 * t + 1];
+        w[nt * stride] = pack_bf16(P[P_W1 + (2 * t) * 32 + o], P[P_W1 + (2 * t + 1) * 32 + o]);
+        b[(nt * 2) * stride] = P[P_B1 + nt * 8 + 2 * t];
+        b[(nt * 2 + 1) * stride] = P[P_B1 + nt * 8 + 2 * t + 1];
+        b[(8 + nt * 2) * stride] = P[P_B2 + nt * 8 + 2 * t];
+        b[(8 + nt * 2 + 1) * stride] = P[P_B2 + nt * 8 + 2 * t + 1];
 #pragma unroll
         for (int ks = 0; ks < 2; ++ks) {
             const int k0 = ks * 16 + 2 * t;
-            F.w2[ks][nt][0] = pack_bf16(P[P_W2 + k0 * 32 + o], P[P_W2 + (k0 + 1) * 32 + o]);
-            F.w2[ks][nt][1] = pack_bf16(P[P_W2 + (k0 + 8) * 32 + o], P[P_W2 + (k0 + 9) * 32 + o]);
+            w[(4 + (ks * 4 + nt) * 2) * stride] =
+                pack_bf16(P[P_W2 + k0 * 32 + o], P[P_W2 + (k0 + 1) * 32 + o]);
+            w[(4 + (ks * 4 + nt) * 2 + 1) * stride] =
+                pack_bf16(P[P_W2 + (k0 + 8) * 32 + o], P[P_W2 + (k0 + 9) * 32 + o]);
         }
     }
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks) {
         const int k0 = ks * 16 + 2 * t;
-        F.w3[ks][0] = g == 0 ? pack_bf16(P[P_W3 + k0], P[P_W3 + k0 + 1]) : 0u;
-        F.w3[ks][1] = g == 0 ? pack_bf16(P[P_W3 + k0 + 8], P[P_W3 + k0 + 9]) : 0u;
+        w[(20 + ks * 2) * stride] = g == 0 ? pack_bf16(P[P_W3 + k0], P[P_W3 + k0 + 1]) : 0u;
+        w[(20 + ks * 2 + 1) * stride] = g == 0 ? pack_bf16(P[P_W3 + k0 + 8], P[P_W3 + k0 + 9]) : 0u;
     }
-    F.b3 = P[P_B3];
+    b[16 * stride] = P[P_B3];
 }
 
 // Scores of the 16 feature rows in smem (row-major [16][16] bf16, columns 8..15 zero); returns
 // the score of row (lane & 15).
-__device__ float mlp16(const __nv_bfloat16* __restrict__ feat, int lane, const MlpFrags& F) {
+template <class Frags>
+__device__ float mlp16(const __nv_bfloat16* __restrict__ feat, int lane, const Frags& F) {
     const int g = lane >> 2, t = lane & 3;
     const uint32_t* row = reinterpret_cast<const uint32_t*>(feat);  // 8 u32 per row
     const uint32_t a0 = row[g * 8 + t], a1 = row[(g + 8) * 8 + t];
     float c1[4][4];
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt) {
-        c1[nt][0] = F.b1[nt][0];
-        c1[nt][1] = F.b1[nt][1];
-        c1[nt][2] = F.b1[nt][0];
-        c1[nt][3] = F.b1[nt][1];
-        mma16816(c1[nt], a0, a1, 0u, 0u, F.w1[nt], 0u);
+        c1[nt][0] = F.b(nt * 2 + 0);
+        c1[nt][1] = F.b(nt * 2 + 1);
+        c1[nt][2] = F.b(nt * 2 + 0);
+        c1[nt][3] = F.b(nt * 2 + 1);
+        mma16816(c1[nt], a0, a1, 0u, 0u, F.w(nt), 0u);
     }
     uint32_t h1[2][4];
 #pragma unroll
@@ -171,14 +189,14 @@ __device__ float mlp16(const __nv_bfloat16* __restrict__ feat, int lane, const M
     float c2[4][4];
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt) {
-        c2[nt][0] = F.b2[nt][0];
-        c2[nt][1] = F.b2[nt][1];
-        c2[nt][2] = F.b2[nt][0];
-        c2[nt][3] = F.b2[nt][1];
+        c2[nt][0] = F.b(8 + nt * 2 + 0);
+        c2[nt][1] = F.b(8 + nt * 2 + 1);
+        c2[nt][2] = F.b(8 + nt * 2 + 0);
+        c2[nt][3] = F.b(8 + nt * 2 + 1);
 #pragma unroll
         for (int ks = 0; ks < 2; ++ks)
-            mma16816(c2[nt], h1[ks][0], h1[ks][1], h1[ks][2], h1[ks][3], F.w2[ks][nt][0],
-                     F.w2[ks][nt][1]);
+            mma16816(c2[nt], h1[ks][0], h1[ks][1], h1[ks][2], h1[ks][3], F.w(4 + (ks * 4 + nt) * 2 + 0),
+                     F.w(4 + (ks * 4 + nt) * 2 + 1));
     }
     uint32_t h2[2][4];
 #pragma unroll
@@ -188,10 +206,10 @@ __device__ float mlp16(const __nv_bfloat16* __restrict__ feat, int lane, const M
         h2[ks][2] = pack_bf16(fmaxf(c2[2 * ks + 1][0], 0.f), fmaxf(c2[2 * ks + 1][1], 0.f));
         h2[ks][3] = pack_bf16(fmaxf(c2[2 * ks + 1][2], 0.f), fmaxf(c2[2 * ks + 1][3], 0.f));
     }
-    float c3[4] = {F.b3, F.b3, F.b3, F.b3};
+    float c3[4] = {F.b(16), F.b(16), F.b(16), F.b(16)};
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks)
-        mma16816(c3, h2[ks][0], h2[ks][1], h2[ks][2], h2[ks][3], F.w3[ks][0], F.w3[ks][1]);
+        mma16816(c3, h2[ks][0], h2[ks][1], h2[ks][2], h2[ks][3], F.w(20 + ks * 2 + 0), F.w(20 + ks * 2 + 1));
     // row r's score sits in lane 4*(r%8): c3[0] for r < 8, c3[2] for r >= 8
     const int r = lane & 15;
     const float v0 = __shfl_sync(0xffffffffu, c3[0], 4 * (r & 7));
@@ -199,15 +217,98 @@ __device__ float mlp16(const __nv_bfloat16* __restrict__ feat, int lane, const M
     return r < 8 ? v0 : v2;
 }
 
+// Scores of 32 feature rows in smem (row-major [32][16] bf16, columns 8..15 zero): the two 16-row
+// blocks go through each layer together, so their mma chains overlap. Returns the score of row
+// `lane`.
+template <class Frags>
+__device__ float mlp32(const __nv_bfloat16* __restrict__ feat, int lane, const Frags& F) {
+    const int g = lane >> 2, t = lane & 3;
+    const uint32_t* row = reinterpret_cast<const uint32_t*>(feat);  // 8 u32 per row
+    uint32_t a0[2], a1[2];
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+        a0[b] = row[(16 * b + g) * 8 + t];
+        a1[b] = row[(16 * b + g + 8) * 8 + t];
+    }
+    float c1[2][4][4];
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            c1[b][nt][0] = F.b(nt * 2 + 0);
+            c1[b][nt][1] = F.b(nt * 2 + 1);
+            c1[b][nt][2] = F.b(nt * 2 + 0);
+            c1[b][nt][3] = F.b(nt * 2 + 1);
+            mma16816(c1[b][nt], a0[b], a1[b], 0u, 0u, F.w(nt), 0u);
+        }
+    uint32_t h[2][2][4];
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks) {
+            h[b][ks][0] = pack_bf16(fmaxf(c1[b][2 * ks][0], 0.f), fmaxf(c1[b][2 * ks][1], 0.f));
+            h[b][ks][1] = pack_bf16(fmaxf(c1[b][2 * ks][2], 0.f), fmaxf(c1[b][2 * ks][3], 0.f));
+            h[b][ks][2] = pack_bf16(fmaxf(c1[b][2 * ks + 1][0], 0.f), fmaxf(c1[b][2 * ks + 1][1], 0.f));
+            h[b][ks][3] = pack_bf16(fmaxf(c1[b][2 * ks + 1][2], 0.f), fmaxf(c1[b][2 * ks + 1][3], 0.f));
+        }
+    float c2[2][4][4];
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            c2[b][nt][0] = F.b(8 + nt * 2 + 0);
+            c2[b][nt][1] = F.b(8 + nt * 2 + 1);
+            c2[b][nt][2] = F.b(8 + nt * 2 + 0);
+            c2[b][nt][3] = F.b(8 + nt * 2 + 1);
+        }
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+                mma16816(c2[b][nt], h[b][ks][0], h[b][ks][1], h[b][ks][2], h[b][ks][3],
+                         F.w(4 + (ks * 4 + nt) * 2 + 0), F.w(4 + (ks * 4 + nt) * 2 + 1));
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks) {
+            h[b][ks][0] = pack_bf16(fmaxf(c2[b][2 * ks][0], 0.f), fmaxf(c2[b][2 * ks][1], 0.f));
+            h[b][ks][1] = pack_bf16(fmaxf(c2[b][2 * ks][2], 0.f), fmaxf(c2[b][2 * ks][3], 0.f));
+            h[b][ks][2] = pack_bf16(fmaxf(c2[b][2 * ks + 1][0], 0.f), fmaxf(c2[b][2 * ks + 1][1], 0.f));
+            h[b][ks][3] = pack_bf16(fmaxf(c2[b][2 * ks + 1][2], 0.f), fmaxf(c2[b][2 * ks + 1][3], 0.f));
+        }
+    float c3[2][4];
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+        c3[b][0] = c3[b][1] = c3[b][2] = c3[b][3] = F.b(16);
+    }
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+            mma16816(c3[b], h[b][ks][0], h[b][ks][1], h[b][ks][2], h[b][ks][3], F.w(20 + ks * 2 + 0),
+                     F.w(20 + ks * 2 + 1));
+    // row r of block b sits in lane 4*(r%8): c3[b][0] for r < 8, c3[b][2] for r >= 8
+    const int r = lane & 15, src = 4 * (r & 7);
+    const float v00 = __shfl_sync(0xffffffffu, c3[0][0], src);
+    const float v02 = __shfl_sync(0xffffffffu, c3[0][2], src);
+    const float v10 = __shfl_sync(0xffffffffu, c3[1][0], src);
+    const float v12 = __shfl_sync(0xffffffffu, c3[1][2], src);
+    return lane < 16 ? (r < 8 ? v00 : v02) : (r < 8 ? v10 : v12);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Learned traversal
 // ---------------------------------------------------------------------------------------------
 constexpr int LT_WARPS = 4;
 constexpr int LT_THREADS = LT_WARPS * 32;
-constexpr int LT_CAP = 1024;  // stack entries per warp
-constexpr int LT_BATCH = 16;
-constexpr uint32_t LT_DIRECT = 16;  // opened cells up to this many bodies: direct sums
-constexpr int LT_LIST = 512;        // interaction list entries per warp
+constexpr int LT_CAP = 1024;        // stack entries per warp
+constexpr int LT_RESERVE = 7 * NB_MAX_TREE_DEPTH + 8;  // headroom of single-cell steps
+constexpr int LT_BATCH = 32;        // cells popped per step (one per lane)
+constexpr uint32_t LT_DIRECT = 8;   // opened cells up to this many bodies: direct sums
+constexpr int LT_LIST = 384;        // interaction list entries per warp (>= LT_BATCH * (LT_DIRECT + 1))
+static_assert(LT_LIST >= LT_BATCH * (LT_DIRECT + 1), "one step must fit in an empty list");
 
 // Sum of the interactions in list[0..count) for one body; 4 independent accumulators. An entry
 // at zero distance (the body itself) contributes nothing.
@@ -244,41 +345,62 @@ __device__ __forceinline__ void flush_list(const float4* __restrict__ list, int 
     oz = (az[0] + az[1]) + (az[2] + az[3]);
 }
 
-__global__ void __launch_bounds__(LT_THREADS)
+__device__ __forceinline__ void two_sum_add(float& h, float& l, float v) {
+    const float s = h + v, bp = s - h;
+    l += (h - (s - bp)) + (v - bp);
+    h = s;
+}
+
+// One warp per group of 32 bodies adjacent in tree order. Each step pops up to 32 cells (one per
+// lane) with their records, extra data and child lists, computes the exact smallest distance
+// from the group to each cell's centre of mass, scores the network's cells with two 16-row BF16
+// mma passes, and then (i) appends accepted monopoles, body leaves and the bodies of small opened
+// cells to the warp's interaction list and (ii) pushes the children of the other opened cells.
+// Interaction-list positions are relative to the group's first body and built from two-float
+// (FP32 value + FP32 residual) coordinates, so nearby pairs keep their full FP32 precision. With
+// params == nullptr the network's cells use the group theta rule instead (same walk, no network).
+__global__ void __launch_bounds__(LT_THREADS, 4)
 bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__ aux,
                   const uint32_t* __restrict__ children, const float4* __restrict__ sorted4,
-                  const uint32_t* __restrict__ info,
-                  const uint32_t* __restrict__ ids, const double* __restrict__ x,
-                  const double* __restrict__ y, const double* __restrict__ z,
-                  const double* __restrict__ box, uint32_t n,
+                  const float4* __restrict__ sorted4lo, uint32_t n,
                   const float* __restrict__ params, float log_tau_scaled, float theta2,
-                  uint32_t count_cap, float eps2, double* __restrict__ ax,
-                  double* __restrict__ ay, double* __restrict__ az,
+                  uint32_t count_cap, float eps2, const uint32_t* __restrict__ ids,
+                  double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az,
                   unsigned long long* __restrict__ counters, uint32_t* __restrict__ err_word) {
     __shared__ uint32_t stack[LT_WARPS][LT_CAP];
     __shared__ __align__(16) __nv_bfloat16 feat[LT_WARPS][LT_BATCH][16];
     __shared__ float4 gpos[LT_WARPS][32];
     __shared__ float4 ilist[LT_WARPS][LT_LIST];
+    __shared__ uint32_t wfrag[MF_W * 32];
+    __shared__ float bfrag[MF_B * 32];
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    if (params != nullptr && wi == 0) load_frags(params, lane, wfrag + lane, bfrag + lane, 32);
+    __syncthreads();  // before any warp leaves
     const uint32_t gw = blockIdx.x * LT_WARPS + wi;
     if (gw * 32 >= n) return;  // whole warp past the end
     const uint32_t p = gw * 32 + lane;
     const bool valid = p < n;
     const uint32_t me = valid ? ids[p] : NB_NONE;
-    const double ox = box[0] + box[6] / 2, oy = box[1] + box[6] / 2, oz = box[2] + box[6] / 2;
-    float px = 0, py = 0, pz = 0, a_prev = 0;
+    // own position: box-centre relative (features) and relative to the group's first body (forces)
+    float4 ph = make_float4(0.f, 0.f, 0.f, 0.f), pl = ph;
+    float a_prev = 0.f;
     if (valid) {
-        px = (float)(x[me] - ox);
-        py = (float)(y[me] - oy);
-        pz = (float)(z[me] - oz);
+        ph = sorted4[p];
+        pl = sorted4lo[p];
         const double a2 = ax[me] * ax[me] + ay[me] * ay[me] + az[me] * az[me];
         a_prev = (float)sqrt(a2);
     }
-    const GroupGeo G = group_geo(valid, px, py, pz, a_prev);
+    const float ghx = __shfl_sync(0xffffffffu, ph.x, 0), ghy = __shfl_sync(0xffffffffu, ph.y, 0),
+                ghz = __shfl_sync(0xffffffffu, ph.z, 0);
+    const float glx = __shfl_sync(0xffffffffu, pl.x, 0), gly = __shfl_sync(0xffffffffu, pl.y, 0),
+                glz = __shfl_sync(0xffffffffu, pl.z, 0);
+    const float px = (ph.x - ghx) + (pl.x - glx), py = (ph.y - ghy) + (pl.y - gly),
+                pz = (ph.z - ghz) + (pl.z - glz);
+    const GroupGeo G = group_geo(valid, ph.x, ph.y, ph.z, a_prev);
     const float inf = __int_as_float(0x7f800000);
-    gpos[wi][lane] = valid ? make_float4(px, py, pz, 0.f) : make_float4(inf, inf, inf, 0.f);
-    MlpFrags F;
-    load_frags(params, lane, F);
+    gpos[wi][lane] = valid ? make_float4(ph.x, ph.y, ph.z, 0.f) : make_float4(inf, inf, inf, 0.f);
+    const bool use_net = params != nullptr;
+    const MlpFragsSmem F{wfrag, bfrag, lane};
     uint32_t* st = stack[wi];
     __nv_bfloat16* fm = &feat[wi][0][0];
     for (int k = lane; k < LT_BATCH * 16; k += 32) fm[k] = __float2bfloat16(0.f);
@@ -286,127 +408,139 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
     int top = 1;
     float hx = 0, hy = 0, hz = 0, lx = 0, ly = 0, lz = 0;
     int list_n = 0;
-    unsigned long long n_acc = 0, n_mlp = 0;
-    __syncwarp();
-    while (top > 0) {
-        int B = min(LT_BATCH, top);
-        B = min(B, (LT_CAP - top) / 7);
-        if (B <= 0) {  // cannot pop without risking overflow: report and stop
-            if (lane == 0) atomicOr(err_word, NB_DEVERR_STACK);
-            break;
-        }
-        uint32_t node = 0;
-        if (lane < B) node = st[top - 1 - lane];
+    unsigned long long n_acc = 0, n_mlp = 0, n_cells = 0, n_steps = 0;
+    NodeRec32 r{};
+    NodeAux xa{};
+    uint4 c0, c1;
+    // Pops the next step's cells and issues their loads. Wide steps keep top <= LT_CAP -
+    // LT_RESERVE; single-cell steps are a plain depth-first walk, which adds at most 7 entries
+    // per tree level, so they stay below LT_CAP.
+    auto pop_and_load = [&]() -> int {
         __syncwarp();
-        top -= B;
-        // lanes i and i+16 load cell i and each scan half of the group for the smallest distance
-        const int ci = lane & 15;
-        const uint32_t cnode = __shfl_sync(0xffffffffu, node, ci);
-        NodeRec32 r{};
-        NodeAux xa{};
+        int nb = top > 0 ? min(min(LT_BATCH, top), max(1, (LT_CAP - LT_RESERVE - top) / 7)) : 0;
+        if (nb > 0 && top + 7 * nb > LT_CAP) {  // unreachable by the bound above; report and stop
+            if (lane == 0) atomicOr(err_word, NB_DEVERR_STACK);
+            nb = 0;
+        }
+        c0 = make_uint4(NB_NONE, NB_NONE, NB_NONE, NB_NONE);
+        c1 = c0;
+        if (lane < nb) {
+            const uint32_t node = st[top - 1 - lane];
+            r = rec[node];
+            xa = aux[node];
+            const uint4* cl = reinterpret_cast<const uint4*>(children + (size_t)node * 8);
+            c0 = cl[0];
+            c1 = cl[1];
+        }
+        __syncwarp();
+        top -= nb;
+        return nb;
+    };
+    int B = pop_and_load();
+    while (B > 0) {
+        const bool live = lane < B;
+        n_cells += (unsigned)B;
+        ++n_steps;
         float m2 = inf;
-        if (ci < B) {
-            r = rec[cnode];
-            const int j0 = (lane >> 4) * 16;
-#pragma unroll 4
-            for (int j = j0; j < j0 + 16; ++j) {
+        if (live) {
+#pragma unroll 8
+            for (int j = 0; j < 32; ++j) {
                 const float4 q = gpos[wi][j];
                 const float dx = r.cx - q.x, dy = r.cy - q.y, dz = r.cz - q.z;
                 m2 = fminf(m2, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
             }
         }
-        m2 = fminf(m2, __shfl_xor_sync(0xffffffffu, m2, 16));
         const float gap = sqrtf(m2);
         int cls = 1;
-        if (lane < B) {
-            xa = aux[node];
+        if (live) {
             float f[NF];
             cls = cell_features(r, xa, G, gap, count_cap, f);
-            if (cls == 0) {
+            if (cls == 0 && use_net) {
 #pragma unroll
                 for (int q = 0; q < NF; ++q) fm[lane * 16 + q] = __float2bfloat16(f[q]);
             }
         }
-        const bool need = lane < B && cls == 0;
-        const unsigned need_mask = __ballot_sync(0xffffffffu, need);
+        const unsigned net_mask = __ballot_sync(0xffffffffu, live && cls == 0);
         float score = 0.f;
-        if (need_mask) {
+        if (use_net && net_mask) {
             __syncwarp();
-            score = mlp16(fm, lane, F);
-            n_mlp += __popc(need_mask);
+            if (net_mask >> 16) {
+                score = mlp32(fm, lane, F);
+            } else {
+                const float v = mlp16(fm, lane, F);
+                if (lane < 16) score = v;
+            }
             __syncwarp();
         }
+        n_mlp += __popc(net_mask);
         bool accept = false;
-        if (lane < B) {
+        if (live) {
             if (cls == 1) accept = true;
-            else if (cls == 0) accept = score < log_tau_scaled;
-            else if (cls == 3)  // group theta rule on the distance to the group's box
-                accept = gap > 0 && r.edge2 < theta2 * gap * gap;
+            else if (cls == 0 && use_net) accept = score < log_tau_scaled;
+            else if (cls != 2)  // group theta rule on the smallest distance
+                accept = gap > 0.f && r.edge2 < theta2 * gap * gap;
         }
-        // accepted monopoles and the bodies of opened cells of at most LT_DIRECT bodies go to the
-        // warp's interaction list, which all lanes sum when it fills
-        const bool direct = lane < B && !accept && xa.count <= LT_DIRECT;
-        const unsigned omask = __ballot_sync(0xffffffffu, lane < B && !accept && !direct);
-        const uint32_t dcount = direct ? xa.count : 0u;
-        uint32_t slots = (accept && lane < B ? 1u : 0u) + dcount;
+        // body leaves and small opened cells: their bodies; other accepted cells: the monopole
+        const bool body_leaf = live && cls == 1;
+        const bool direct = body_leaf || (live && !accept && xa.count <= LT_DIRECT);
+        const bool mono = live && accept && !body_leaf;
+        const bool open = live && !accept && !direct;
+        // push the children of opened cells (8-entry child lists, NB_NONE padded)
+        {
+            uint32_t nchild = 0;
+            if (open) {
+                const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+#pragma unroll
+                for (int q = 0; q < 8; ++q) nchild += v[q] != NB_NONE;
+            }
+            uint32_t off = nchild;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, off, o);
+                if (lane >= o) off += v;
+            }
+            const uint32_t total = __shfl_sync(0xffffffffu, off, 31);
+            off -= nchild;
+            if (nchild) {
+                const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (q < (int)nchild) st[top + off + q] = v[q];
+            }
+            top += (int)total;
+        }
+        // what the interaction list needs from this step, before the next step's loads land
+        const float4 mono_e = make_float4((r.cx - ghx) - glx, (r.cy - ghy) - gly,
+                                          (r.cz - ghz) - glz, r.gm);
+        const uint32_t d_first = xa.first, d_count = direct ? xa.count : 0u;
+        const uint32_t slots = direct ? d_count : (mono ? 1u : 0u);
         uint32_t pos = slots;
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t v = __shfl_up_sync(0xffffffffu, pos, o);
             if (lane >= o) pos += v;
         }
-        const uint32_t batch_total = __shfl_sync(0xffffffffu, pos, 31);
+        const uint32_t step_total = __shfl_sync(0xffffffffu, pos, 31);
         pos -= slots;
-        if (list_n + (int)batch_total > LT_LIST) {  // make room: sum the list so far
-            __syncwarp();
+        B = pop_and_load();  // next step's cells are in flight during the list work below
+        if (list_n + (int)step_total > LT_LIST) {  // make room: sum the list so far
             float fx, fy, fz;
             flush_list(ilist[wi], list_n, px, py, pz, eps2, fx, fy, fz);
             if (valid) {
-                float sh = hx + fx, bp = sh - hx;
-                lx += (hx - (sh - bp)) + (fx - bp);
-                hx = sh;
-                sh = hy + fy;
-                bp = sh - hy;
-                ly += (hy - (sh - bp)) + (fy - bp);
-                hy = sh;
-                sh = hz + fz;
-                bp = sh - hz;
-                lz += (hz - (sh - bp)) + (fz - bp);
-                hz = sh;
+                two_sum_add(hx, lx, fx);
+                two_sum_add(hy, ly, fy);
+                two_sum_add(hz, lz, fz);
             }
             list_n = 0;
             __syncwarp();
         }
-        if (lane < B && accept) ilist[wi][list_n + pos] = make_float4(r.cx, r.cy, r.cz, r.gm);
-        for (uint32_t j = 0; j < dcount; ++j)
-            ilist[wi][list_n + pos + (accept && lane < B ? 1u : 0u) + j] = sorted4[xa.first + j];
-        list_n += (int)batch_total;
-        n_acc += batch_total;
-        __syncwarp();
-        // push the children of opened cells (8-entry child lists, NB_NONE padded)
-        uint4 c0 = make_uint4(NB_NONE, NB_NONE, NB_NONE, NB_NONE), c1 = c0;
-        uint32_t nchild = 0;
-        if ((omask >> lane) & 1u) {
-            const uint4* cl = reinterpret_cast<const uint4*>(children + (size_t)node * 8);
-            c0 = cl[0];
-            c1 = cl[1];
-            const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-#pragma unroll
-            for (int q = 0; q < 8; ++q) nchild += v[q] != NB_NONE;
+        float4* L = ilist[wi] + list_n + pos;
+        if (mono) L[0] = mono_e;
+        for (uint32_t j = 0; j < d_count; ++j) {
+            const float4 h = sorted4[d_first + j], l = sorted4lo[d_first + j];
+            L[j] = make_float4((h.x - ghx) + (l.x - glx), (h.y - ghy) + (l.y - gly),
+                               (h.z - ghz) + (l.z - glz), h.w);
         }
-        uint32_t off = nchild;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, off, o);
-            if (lane >= o) off += v;
-        }
-        const uint32_t total = __shfl_sync(0xffffffffu, off, 31);
-        off -= nchild;
-        if (nchild) {
-            const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (q < (int)nchild) st[top + off + q] = v[q];
-        }
-        top += (int)total;
+        list_n += (int)step_total;
+        n_acc += step_total;
         __syncwarp();
     }
     __syncwarp();
@@ -421,6 +555,8 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
     if (counters && lane == 0) {
         atomicAdd(&counters[0], n_acc * (unsigned long long)valid_lanes);
         atomicAdd(&counters[1], n_mlp);
+        atomicAdd(&counters[2], n_cells);
+        atomicAdd(&counters[3], n_steps);
     }
 }
 
@@ -690,24 +826,29 @@ __global__ void mlp_predict_kernel(const float* __restrict__ P, const float* __r
     out[s] = res;
 }
 
-// BF16 tensor-core inference of the same network (16 rows per warp), for validating mlp16.
+// BF16 tensor-core inference of the same network as the traversal runs it (weight fragments in
+// shared memory, 32 rows per warp step through mlp32, a last step of at most 16 rows through
+// mlp16), for validating both against the FP32 network.
 __global__ void __launch_bounds__(128)
 mlp_predict_bf16_kernel(const float* __restrict__ P, const float* __restrict__ X, uint32_t n,
                         float* __restrict__ out) {
-    __shared__ __align__(16) __nv_bfloat16 feat[4][16][16];
+    __shared__ __align__(16) __nv_bfloat16 feat[4][32][16];
+    __shared__ uint32_t wsm[MF_W * 32];
+    __shared__ float bsm[MF_B * 32];
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
-    MlpFrags F;
-    load_frags(P, lane, F);
+    if (wi == 0) load_frags(P, lane, wsm + lane, bsm + lane, 32);
+    __syncthreads();
+    const MlpFragsSmem F{wsm, bsm, lane};
     __nv_bfloat16* fm = &feat[wi][0][0];
-    for (uint32_t base = (blockIdx.x * 4 + wi) * 16; base < n; base += gridDim.x * 4 * 16) {
-        for (int k = lane; k < 256; k += 32) {
+    for (uint32_t base = (blockIdx.x * 4 + wi) * 32; base < n; base += gridDim.x * 4 * 32) {
+        for (int k = lane; k < 512; k += 32) {
             const uint32_t r = base + k / 16;
             const int c = k % 16;
             fm[k] = __float2bfloat16(c < NF && r < n ? X[(size_t)r * NF + c] : 0.f);
         }
         __syncwarp();
-        const float s = mlp16(fm, lane, F);
-        if (lane < 16 && base + lane < n) out[base + lane] = s;
+        const float v = n - base > 16 ? mlp32(fm, lane, F) : mlp16(fm, lane, F);
+        if (base + lane < n && (n - base > 16 || lane < 16)) out[base + lane] = v;
         __syncwarp();
     }
 }
@@ -757,7 +898,7 @@ nb_status nb_mlp_predict(nb_ctx* ctx, const float* params, const float* X, uint3
     if (n == 0) return NB_OK;
     cudaStream_t s = (cudaStream_t)stream;
     if (bf16_tensor_cores) {
-        int blocks = nb::ceil_div(n, 64);
+        int blocks = nb::ceil_div(n, 128);
         if (blocks > ctx->sm_count * 8) blocks = ctx->sm_count * 8;
         mlp_predict_bf16_kernel<<<blocks, 128, 0, s>>>(params, X, n, out);
         return nb::check_launch("mlp_predict_bf16_kernel");
@@ -770,6 +911,7 @@ nb_status nb_bh_set_policy(nb_bh_tree* t, const float* params_dev, float log10_t
                            double theta_fallback, uint32_t count_cap) {
     if (!t) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_set_policy: null tree");
     t->policy = params_dev;
+    t->policy_set = true;
     t->policy_log_tau = log10_tau;
     t->policy_theta = (float)theta_fallback;
     t->policy_count_cap = count_cap;
@@ -816,13 +958,13 @@ namespace nb {
 nb_status launch_learned(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const double* y,
                          const double* z, double* ax, double* ay, double* az, double eps2,
                          unsigned long long* counters, cudaStream_t s) {
-    if (!t->policy)
+    if (!t->policy_set)
         return set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: NB_OPEN_LEARNED needs nb_bh_set_policy");
     const uint32_t warps = (t->n + 31) / 32;
     bh_learned_kernel<<<ceil_div(warps, LT_WARPS), LT_THREADS, 0, s>>>(
-        t->rec32, t->aux, t->children, t->sorted4, t->info, t->ids, x, y, z, t->box, t->n, t->policy,
+        t->rec32, t->aux, t->children, t->sorted4, t->sorted4lo, t->n, t->policy,
         t->policy_log_tau * 0.2f, t->policy_theta * t->policy_theta, t->policy_count_cap,
-        (float)eps2, ax, ay, az, counters, ctx->dev_error);
+        (float)eps2, t->ids, ax, ay, az, counters, ctx->dev_error);
     return check_launch("bh_learned_kernel");
 }
 

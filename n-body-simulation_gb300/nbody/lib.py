@@ -296,14 +296,16 @@ class BHTree:
                                         count_cap))
 
     def accel_learned_counted(self, x, y, z, ax, ay, az, eps2, stream=None):
+        """NB_OPEN_LEARNED traversal; returns (interactions, policy decisions, cells visited,
+        walk steps)."""
         import torch
-        cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        cnt = torch.zeros(4, dtype=torch.int64, device="cuda")
         check(self.lib.nb_bh_accel_learned_counted(self.ctx.handle, self.handle, ptr(x), ptr(y),
                                                    ptr(z), ptr(ax), ptr(ay), ptr(az), eps2,
                                                    ptr(cnt), stream_ptr(stream)))
         self.ctx.sync(stream)
-        a, b = cnt.cpu().tolist()
-        return int(a), int(b)
+        a, b, c, d = cnt.cpu().tolist()
+        return int(a), int(b), int(c), int(d)
 
     def generate_pairs(self, m, x, y, z, ax, ay, az, G, eps2, theta_gen, sample_fraction, seed,
                        count_cap, max_pairs, with_ids=False, stream=None):

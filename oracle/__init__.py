@@ -2,7 +2,7 @@
 
 A ctypes binding of ``oracle/nbody_oracle.cpp``, a C++17/OpenMP restatement of the reference's
 kernels (file:line citations in that file). Only ``tests/``, ``__graft_entry__.smoke()`` and the
-CPU legs of ``bench.py`` import this package, and only as the checker or the timed CPU baseline;
+CPU legs of ``bench.py`` import this package, and only as the parity reference or the timed CPU baseline;
 the CUDA library and the host driver never load it.
 
 Pinned against the reference's own known answers (tests/BarnesHutTest.cpp): AABB, node table,

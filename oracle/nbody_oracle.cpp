@@ -1,7 +1,7 @@
 // nbody_oracle.cpp -- CPU ORACLE (test infrastructure only).
 //
 // A C++17/OpenMP restatement of TimThuering/N-Body-Simulation's two force paths, used as the
-// checker for the CUDA library and as the timed CPU baseline. It is never linked into, loaded by,
+// parity reference for the CUDA library and as the timed CPU baseline. It is never linked into, loaded by,
 // or called from the product path (the CUDA library and the host driver); only tests/, the smoke
 // check and bench.py's CPU legs load it.
 //
