@@ -385,10 +385,12 @@ def run_ours(args):
 
 
 def secondary_measurements(ctx, tree, m, pos, acc, G):
-    """Other configurations' throughput on the same GPU (short runs)."""
+    """The other workloads on the same GPU: the FP32-pair group-rule step on the headline state,
+    the reference's CPU-path configuration (naive FP64, 16,384-body disc), and the precision,
+    batched and learned forms of the method (nbody/workloads.py)."""
     import torch
 
-    from nbody import generators
+    from nbody import generators, workloads
     from nbody.lib import fma_peak
 
     out = {}
@@ -411,21 +413,22 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
         tree.accel(*pos, *acc, G, EPS2, "group", "f32c")
     ms = timed(bh32, 10)
     out["bh_f32c_group_theta0.5_1M"] = {"build_plus_traversal_ms": ms, "steps_per_s": 1e3 / ms}
-    fp32_peak = fma_peak(ctx, fp64=False)
-    # naive FP32-compensated, N = 262,144 Plummer (config 3 shape)
-    for name, n, prec, reps, kind in (("naive_f32c_plummer_262144", 262144, "f32c", 5, "plummer"),
-                                      ("naive_f64_disc_16384", 16384, "f64", 5, "disc")):
-        dd = generators.plummer(n, 1) if kind == "plummer" else generators.heliocentric_disc(n, 1)
-        t = {k: torch.as_tensor(dd[k], device="cuda") for k in ("m", "x", "y", "z")}
-        a = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(3)]
-        eps2 = 1e-6 if kind == "plummer" else EPS2
-        ms = timed(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, dd["G"], eps2, prec),
-                   reps)
-        gp = n * n / (ms * 1e-3) / 1e9
-        peak = fp32_peak if prec == "f32c" else fma_peak(ctx, fp64=True)
-        out[name] = {"ms_per_eval": ms, "gpairs_per_s": gp, "tflops_20_per_pair": gp * 20 / 1e3,
-                     "frac_of_measured_fma_peak": gp * 20e9 / peak}
-    out["fp32_fma_peak_tflops"] = fp32_peak / 1e12
+    # naive FP64 on the reference's CPU-path configuration (16,384-body disc)
+    n = 16384
+    dd = generators.heliocentric_disc(n, 1)
+    t = {k: torch.as_tensor(dd[k], device="cuda") for k in ("m", "x", "y", "z")}
+    a = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    ms = timed(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, dd["G"], EPS2, "f64"), 5)
+    gp = n * n / (ms * 1e-3) / 1e9
+    out["naive_f64_disc_16384"] = {"ms_per_eval": ms, "gpairs_per_s": gp,
+                                   "frac_of_measured_fp64_fma_peak":
+                                       gp * 20e9 / fma_peak(ctx, fp64=True)}
+    for name, fn in (("precision_form_naive_f32c_plummer_262144", workloads.precision_form),
+                     ("batched_ensemble_512_plummer", workloads.batched_ensemble),
+                     ("learned_opening_bh_mix_1M", workloads.learned_form)):
+        t0 = time.perf_counter()
+        out[name] = fn(ctx)
+        out[name]["wall_s"] = time.perf_counter() - t0
     return out
 
 

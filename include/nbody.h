@@ -330,9 +330,13 @@ nb_status nb_bh_generate_pairs(nb_ctx* ctx, const nb_bh_tree* tree, const double
  * cells with more than count_cap bodies use the group theta rule with theta_fallback. The
  * traversal reads |a| of the previous step from the ax, ay, az arrays it then overwrites.
  * params_dev NULL selects the same walk with the group theta rule (theta_fallback) in place of
- * the network: the method without it. */
+ * the network: the method without it.
+ * flags: NB_POLICY_BOUND_ACCEPT accepts, before the network is asked, every cell whose analytic
+ * monopole error bound (multipole series, bodies within sqrt(3) * edge of the centre of mass)
+ * relative to the group's smallest |a| is below tau. */
+#define NB_POLICY_BOUND_ACCEPT 1u
 nb_status nb_bh_set_policy(nb_bh_tree* tree, const float* params_dev, float log10_tau,
-                           double theta_fallback, uint32_t count_cap);
+                           double theta_fallback, uint32_t count_cap, uint32_t flags);
 /* NB_OPEN_LEARNED traversal that also counts, into 4 DEVICE uint64: body-cell interactions
  * (counters_dev[0]), cells decided by the policy (network, or theta rule when the policy has no
  * network) ([1]), cells visited ([2]) and walk steps of up to 32 cells ([3]), summed over groups. */

@@ -391,6 +391,7 @@ void carve(nb_bh_tree* t, Carver& c) {
     const size_t n = t->n_max, cap = t->node_cap;
     t->box = c.take<double>(16);
     t->info = c.take<uint32_t>(16);
+    t->work = c.take<uint32_t>(16);
     t->key0 = c.take<uint64_t>(n);
     t->key1 = c.take<uint64_t>(n);
     t->key_alt = c.take<uint64_t>(n);

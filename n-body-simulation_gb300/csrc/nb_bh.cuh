@@ -47,6 +47,7 @@ struct nb_bh_tree {
 
     double* box = nullptr;  // [0..6] AABB (min xyz, max xyz, edge), [7..9] box centre
     uint32_t* info = nullptr;  // [0] node count (copy of base[n])
+    uint32_t* work = nullptr;  // work counter of persistent traversal kernels
 
     uint64_t *key0 = nullptr, *key1 = nullptr, *key_alt = nullptr;
     uint32_t *ids = nullptr, *ids_alt = nullptr;
@@ -72,6 +73,7 @@ struct nb_bh_tree {
     // learned opening policy (device parameters, see nb_learned.cu)
     const float* policy = nullptr;  // nullptr after nb_bh_set_policy: theta rule, same walk
     bool policy_set = false;
+    uint32_t policy_flags = 0;
     float policy_log_tau = 0.f;
     float policy_theta = 0.5f;
     uint32_t policy_count_cap = 8192;

@@ -65,16 +65,27 @@ __device__ GroupGeo group_geo(bool valid, float px, float py, float pz, float a_
 
 // The 8 features of a (group, cell) pair and the cell's class: 0 = decide with the network,
 // 1 = body leaf (accept), 2 = may overlap the group (open), 3 = outside the training range
-// (theta rule). gap = the smallest distance from a member of the group to the cell's centre of
+// (theta rule), 4 = provably accurate enough (accept). gap = the smallest distance from a member of the group to the cell's centre of
 // mass; d = distance from the group's box centre. Ratios use the fast reciprocal and logarithms
 // the fast base-2 logarithm (features only steer the policy; labels and training use the same
 // function).
+//
+// Class 4 (accept without the network; only when bound_tau > 0): the cell's bodies lie within
+// b = sqrt(3) * edge of its centre of mass, so for a body at distance R >= gap the monopole's
+// force error is at most G M / R^2 * sum_{l>=2} (l+1) (b/R)^l = G M / R^2 * (1/(1-rho)^2 - 1 -
+// 2 rho), rho = b / gap (the multipole series of the potential with a vanishing dipole). When
+// that bound relative to the group's smallest |a| is below bound_tau the cell is accepted.
 __device__ __forceinline__ int cell_features(const NodeRec32& r, const NodeAux& x,
                                              const GroupGeo& g, float gap, uint32_t count_cap,
-                                             float* f) {
+                                             float* f, float bound_tau = 0.f) {
     if (r.body != NB_NONE) return 1;
     const float e = x.edge;
     if (gap <= SQRT3 * e) return 2;
+    if (bound_tau > 0.f) {
+        const float rho = __fdividef(SQRT3 * e, gap), q = 1.f - rho;
+        const float tail = __fdividef(1.f, q * q) - 1.f - 2.f * rho;
+        if (__fdividef(r.gm, gap * gap * g.a_ref) * tail < bound_tau) return 4;
+    }
     if (x.count > count_cap) return 3;
     const float dx = r.cx - g.cx, dy = r.cy - g.cy, dz = r.cz - g.cz;
     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
@@ -359,14 +370,16 @@ __device__ __forceinline__ void two_sum_add(float& h, float& l, float v) {
 // Interaction-list positions are relative to the group's first body and built from two-float
 // (FP32 value + FP32 residual) coordinates, so nearby pairs keep their full FP32 precision. With
 // params == nullptr the network's cells use the group theta rule instead (same walk, no network).
+template <bool COUNTED>
 __global__ void __launch_bounds__(LT_THREADS, 4)
 bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__ aux,
                   const uint32_t* __restrict__ children, const float4* __restrict__ sorted4,
                   const float4* __restrict__ sorted4lo, uint32_t n,
-                  const float* __restrict__ params, float log_tau_scaled, float theta2,
-                  uint32_t count_cap, float eps2, const uint32_t* __restrict__ ids,
+                  const float* __restrict__ params, float log_tau_scaled, float bound_tau,
+                  float theta2, uint32_t count_cap, float eps2, const uint32_t* __restrict__ ids,
                   double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az,
-                  unsigned long long* __restrict__ counters, uint32_t* __restrict__ err_word) {
+                  unsigned long long* __restrict__ counters, uint32_t* __restrict__ err_word,
+                  uint32_t* __restrict__ next_group) {
     __shared__ uint32_t stack[LT_WARPS][LT_CAP];
     __shared__ __align__(16) __nv_bfloat16 feat[LT_WARPS][LT_BATCH][16];
     __shared__ float4 gpos[LT_WARPS][32];
@@ -376,187 +389,203 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
     if (params != nullptr && wi == 0) load_frags(params, lane, wfrag + lane, bfrag + lane, 32);
     __syncthreads();  // before any warp leaves
-    const uint32_t gw = blockIdx.x * LT_WARPS + wi;
-    if (gw * 32 >= n) return;  // whole warp past the end
-    const uint32_t p = gw * 32 + lane;
-    const bool valid = p < n;
-    const uint32_t me = valid ? ids[p] : NB_NONE;
-    // own position: box-centre relative (features) and relative to the group's first body (forces)
-    float4 ph = make_float4(0.f, 0.f, 0.f, 0.f), pl = ph;
-    float a_prev = 0.f;
-    if (valid) {
-        ph = sorted4[p];
-        pl = sorted4lo[p];
-        const double a2 = ax[me] * ax[me] + ay[me] * ay[me] + az[me] * az[me];
-        a_prev = (float)sqrt(a2);
-    }
-    const float ghx = __shfl_sync(0xffffffffu, ph.x, 0), ghy = __shfl_sync(0xffffffffu, ph.y, 0),
-                ghz = __shfl_sync(0xffffffffu, ph.z, 0);
-    const float glx = __shfl_sync(0xffffffffu, pl.x, 0), gly = __shfl_sync(0xffffffffu, pl.y, 0),
-                glz = __shfl_sync(0xffffffffu, pl.z, 0);
-    const float px = (ph.x - ghx) + (pl.x - glx), py = (ph.y - ghy) + (pl.y - gly),
-                pz = (ph.z - ghz) + (pl.z - glz);
-    const GroupGeo G = group_geo(valid, ph.x, ph.y, ph.z, a_prev);
-    const float inf = __int_as_float(0x7f800000);
-    gpos[wi][lane] = valid ? make_float4(ph.x, ph.y, ph.z, 0.f) : make_float4(inf, inf, inf, 0.f);
-    const bool use_net = params != nullptr;
-    const MlpFragsSmem F{wfrag, bfrag, lane};
-    uint32_t* st = stack[wi];
-    __nv_bfloat16* fm = &feat[wi][0][0];
-    for (int k = lane; k < LT_BATCH * 16; k += 32) fm[k] = __float2bfloat16(0.f);
-    if (lane == 0) st[0] = 0;
-    int top = 1;
-    float hx = 0, hy = 0, hz = 0, lx = 0, ly = 0, lz = 0;
-    int list_n = 0;
-    unsigned long long n_acc = 0, n_mlp = 0, n_cells = 0, n_steps = 0;
-    NodeRec32 r{};
-    NodeAux xa{};
-    uint4 c0, c1;
-    // Pops the next step's cells and issues their loads. Wide steps keep top <= LT_CAP -
-    // LT_RESERVE; single-cell steps are a plain depth-first walk, which adds at most 7 entries
-    // per tree level, so they stay below LT_CAP.
-    auto pop_and_load = [&]() -> int {
-        __syncwarp();
-        int nb = top > 0 ? min(min(LT_BATCH, top), max(1, (LT_CAP - LT_RESERVE - top) / 7)) : 0;
-        if (nb > 0 && top + 7 * nb > LT_CAP) {  // unreachable by the bound above; report and stop
-            if (lane == 0) atomicOr(err_word, NB_DEVERR_STACK);
-            nb = 0;
+    const uint32_t n_groups = (n + 31) / 32;
+    unsigned long long t_acc = 0, t_mlp = 0, t_cells = 0, t_steps = 0;
+    // persistent warps: each takes the next group until none are left (no warp idles while its
+    // block's other warps finish long walks)
+    for (;;) {
+        uint32_t gw = 0;
+        if (lane == 0) gw = atomicAdd(next_group, 1u);
+        gw = __shfl_sync(0xffffffffu, gw, 0);
+        if (gw >= n_groups) break;
+        const uint32_t p = gw * 32 + lane;
+        const bool valid = p < n;
+        const uint32_t me = valid ? ids[p] : NB_NONE;
+        // own position: box-centre relative (features) and relative to the group's first body (forces)
+        float4 ph = make_float4(0.f, 0.f, 0.f, 0.f), pl = ph;
+        float a_prev = 0.f;
+        if (valid) {
+            ph = sorted4[p];
+            pl = sorted4lo[p];
+            const double a2 = ax[me] * ax[me] + ay[me] * ay[me] + az[me] * az[me];
+            a_prev = (float)sqrt(a2);
         }
-        c0 = make_uint4(NB_NONE, NB_NONE, NB_NONE, NB_NONE);
-        c1 = c0;
-        if (lane < nb) {
-            const uint32_t node = st[top - 1 - lane];
-            r = rec[node];
-            xa = aux[node];
-            const uint4* cl = reinterpret_cast<const uint4*>(children + (size_t)node * 8);
-            c0 = cl[0];
-            c1 = cl[1];
-        }
-        __syncwarp();
-        top -= nb;
-        return nb;
-    };
-    int B = pop_and_load();
-    while (B > 0) {
-        const bool live = lane < B;
-        n_cells += (unsigned)B;
-        ++n_steps;
-        float m2 = inf;
-        if (live) {
-#pragma unroll 8
-            for (int j = 0; j < 32; ++j) {
-                const float4 q = gpos[wi][j];
-                const float dx = r.cx - q.x, dy = r.cy - q.y, dz = r.cz - q.z;
-                m2 = fminf(m2, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-            }
-        }
-        const float gap = sqrtf(m2);
-        int cls = 1;
-        if (live) {
-            float f[NF];
-            cls = cell_features(r, xa, G, gap, count_cap, f);
-            if (cls == 0 && use_net) {
-#pragma unroll
-                for (int q = 0; q < NF; ++q) fm[lane * 16 + q] = __float2bfloat16(f[q]);
-            }
-        }
-        const unsigned net_mask = __ballot_sync(0xffffffffu, live && cls == 0);
-        float score = 0.f;
-        if (use_net && net_mask) {
+        const float ghx = __shfl_sync(0xffffffffu, ph.x, 0), ghy = __shfl_sync(0xffffffffu, ph.y, 0),
+                    ghz = __shfl_sync(0xffffffffu, ph.z, 0);
+        const float glx = __shfl_sync(0xffffffffu, pl.x, 0), gly = __shfl_sync(0xffffffffu, pl.y, 0),
+                    glz = __shfl_sync(0xffffffffu, pl.z, 0);
+        const float px = (ph.x - ghx) + (pl.x - glx), py = (ph.y - ghy) + (pl.y - gly),
+                    pz = (ph.z - ghz) + (pl.z - glz);
+        const GroupGeo G = group_geo(valid, ph.x, ph.y, ph.z, a_prev);
+        const float inf = __int_as_float(0x7f800000);
+        gpos[wi][lane] = valid ? make_float4(ph.x, ph.y, ph.z, 0.f) : make_float4(inf, inf, inf, 0.f);
+        const bool use_net = params != nullptr;
+        const MlpFragsSmem F{wfrag, bfrag, lane};
+        uint32_t* st = stack[wi];
+        __nv_bfloat16* fm = &feat[wi][0][0];
+        for (int k = lane; k < LT_BATCH * 16; k += 32) fm[k] = __float2bfloat16(0.f);
+        if (lane == 0) st[0] = 0;
+        int top = 1;
+        float hx = 0, hy = 0, hz = 0, lx = 0, ly = 0, lz = 0;
+        int list_n = 0;
+        uint32_t n_acc = 0, n_mlp = 0, n_cells = 0, n_steps = 0;  // COUNTED only
+        NodeRec32 r{};
+        NodeAux xa{};
+        uint4 c0, c1;
+        // Pops the next step's cells and issues their loads. Wide steps keep top <= LT_CAP -
+        // LT_RESERVE; single-cell steps are a plain depth-first walk, which adds at most 7 entries
+        // per tree level, so they stay below LT_CAP.
+        auto pop_and_load = [&]() -> int {
             __syncwarp();
-            if (net_mask >> 16) {
-                score = mlp32(fm, lane, F);
-            } else {
-                const float v = mlp16(fm, lane, F);
-                if (lane < 16) score = v;
+            int nb = top > 0 ? min(min(LT_BATCH, top), max(1, (LT_CAP - LT_RESERVE - top) / 7)) : 0;
+            if (nb > 0 && top + 7 * nb > LT_CAP) {  // unreachable by the bound above; report and stop
+                if (lane == 0) atomicOr(err_word, NB_DEVERR_STACK);
+                nb = 0;
+            }
+            c0 = make_uint4(NB_NONE, NB_NONE, NB_NONE, NB_NONE);
+            c1 = c0;
+            if (lane < nb) {
+                const uint32_t node = st[top - 1 - lane];
+                r = rec[node];
+                xa = aux[node];
+                const uint4* cl = reinterpret_cast<const uint4*>(children + (size_t)node * 8);
+                c0 = cl[0];
+                c1 = cl[1];
             }
             __syncwarp();
-        }
-        n_mlp += __popc(net_mask);
-        bool accept = false;
-        if (live) {
-            if (cls == 1) accept = true;
-            else if (cls == 0 && use_net) accept = score < log_tau_scaled;
-            else if (cls != 2)  // group theta rule on the smallest distance
-                accept = gap > 0.f && r.edge2 < theta2 * gap * gap;
-        }
-        // body leaves and small opened cells: their bodies; other accepted cells: the monopole
-        const bool body_leaf = live && cls == 1;
-        const bool direct = body_leaf || (live && !accept && xa.count <= LT_DIRECT);
-        const bool mono = live && accept && !body_leaf;
-        const bool open = live && !accept && !direct;
-        // push the children of opened cells (8-entry child lists, NB_NONE padded)
-        {
-            uint32_t nchild = 0;
-            if (open) {
-                const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-#pragma unroll
-                for (int q = 0; q < 8; ++q) nchild += v[q] != NB_NONE;
+            top -= nb;
+            return nb;
+        };
+        int B = pop_and_load();
+        while (B > 0) {
+            const bool live = lane < B;
+            if (COUNTED) {
+                n_cells += (unsigned)B;
+                ++n_steps;
             }
-            uint32_t off = nchild;
+            float m2 = inf;
+            if (live) {
+    #pragma unroll 8
+                for (int j = 0; j < 32; ++j) {
+                    const float4 q = gpos[wi][j];
+                    const float dx = r.cx - q.x, dy = r.cy - q.y, dz = r.cz - q.z;
+                    m2 = fminf(m2, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                }
+            }
+            const float gap = sqrtf(m2);
+            int cls = 1;
+            uint4 fv = make_uint4(0u, 0u, 0u, 0u);  // the features as BF16 pairs
+            if (live) {
+                float f[NF];
+                cls = cell_features(r, xa, G, gap, count_cap, f, bound_tau);
+                fv = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]),
+                                pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+            }
+            // the network's cells are packed into the first rows of the feature tile
+            const unsigned net_mask = __ballot_sync(0xffffffffu, live && cls == 0);
+            const int row = __popc(net_mask & ((1u << lane) - 1u));
+            const int rows = __popc(net_mask);
+            float score = 0.f;
+            if (use_net && rows) {
+                if (live && cls == 0) *reinterpret_cast<uint4*>(fm + row * 16) = fv;
+                __syncwarp();
+                const float v = rows > 16 ? mlp32(fm, lane, F) : mlp16(fm, lane, F);
+                score = __shfl_sync(0xffffffffu, v, row & 31);
+                __syncwarp();
+            }
+            if (COUNTED) n_mlp += rows;
+            bool accept = false;
+            if (live) {
+                if (cls == 1 || cls == 4) accept = true;
+                else if (cls == 0 && use_net) accept = score < log_tau_scaled;
+                else if (cls != 2)  // group theta rule on the smallest distance
+                    accept = gap > 0.f && r.edge2 < theta2 * gap * gap;
+            }
+            // body leaves and small opened cells: their bodies; other accepted cells: the monopole
+            const bool body_leaf = live && cls == 1;
+            const bool direct = body_leaf || (live && !accept && xa.count <= LT_DIRECT);
+            const bool mono = live && accept && !body_leaf;
+            const bool open = live && !accept && !direct;
+            // push the children of opened cells (8-entry child lists, NB_NONE padded)
+            {
+                uint32_t nchild = 0;
+                if (open) {
+                    const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+    #pragma unroll
+                    for (int q = 0; q < 8; ++q) nchild += v[q] != NB_NONE;
+                }
+                uint32_t off = nchild;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t v = __shfl_up_sync(0xffffffffu, off, o);
+                    if (lane >= o) off += v;
+                }
+                const uint32_t total = __shfl_sync(0xffffffffu, off, 31);
+                off -= nchild;
+                if (nchild) {
+                    const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+    #pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        if (q < (int)nchild) st[top + off + q] = v[q];
+                }
+                top += (int)total;
+            }
+            // what the interaction list needs from this step, before the next step's loads land
+            const float4 mono_e = make_float4((r.cx - ghx) - glx, (r.cy - ghy) - gly,
+                                              (r.cz - ghz) - glz, r.gm);
+            const uint32_t d_first = xa.first, d_count = direct ? xa.count : 0u;
+            const uint32_t slots = direct ? d_count : (mono ? 1u : 0u);
+            uint32_t pos = slots;
             for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t v = __shfl_up_sync(0xffffffffu, off, o);
-                if (lane >= o) off += v;
+                const uint32_t v = __shfl_up_sync(0xffffffffu, pos, o);
+                if (lane >= o) pos += v;
             }
-            const uint32_t total = __shfl_sync(0xffffffffu, off, 31);
-            off -= nchild;
-            if (nchild) {
-                const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-#pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (q < (int)nchild) st[top + off + q] = v[q];
+            const uint32_t step_total = __shfl_sync(0xffffffffu, pos, 31);
+            pos -= slots;
+            B = pop_and_load();  // next step's cells are in flight during the list work below
+            if (list_n + (int)step_total > LT_LIST) {  // make room: sum the list so far
+                float fx, fy, fz;
+                flush_list(ilist[wi], list_n, px, py, pz, eps2, fx, fy, fz);
+                if (valid) {
+                    two_sum_add(hx, lx, fx);
+                    two_sum_add(hy, ly, fy);
+                    two_sum_add(hz, lz, fz);
+                }
+                list_n = 0;
+                __syncwarp();
             }
-            top += (int)total;
-        }
-        // what the interaction list needs from this step, before the next step's loads land
-        const float4 mono_e = make_float4((r.cx - ghx) - glx, (r.cy - ghy) - gly,
-                                          (r.cz - ghz) - glz, r.gm);
-        const uint32_t d_first = xa.first, d_count = direct ? xa.count : 0u;
-        const uint32_t slots = direct ? d_count : (mono ? 1u : 0u);
-        uint32_t pos = slots;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, pos, o);
-            if (lane >= o) pos += v;
-        }
-        const uint32_t step_total = __shfl_sync(0xffffffffu, pos, 31);
-        pos -= slots;
-        B = pop_and_load();  // next step's cells are in flight during the list work below
-        if (list_n + (int)step_total > LT_LIST) {  // make room: sum the list so far
-            float fx, fy, fz;
-            flush_list(ilist[wi], list_n, px, py, pz, eps2, fx, fy, fz);
-            if (valid) {
-                two_sum_add(hx, lx, fx);
-                two_sum_add(hy, ly, fy);
-                two_sum_add(hz, lz, fz);
+            float4* L = ilist[wi] + list_n + pos;
+            if (mono) L[0] = mono_e;
+            for (uint32_t j = 0; j < d_count; ++j) {
+                const float4 h = sorted4[d_first + j], l = sorted4lo[d_first + j];
+                L[j] = make_float4((h.x - ghx) + (l.x - glx), (h.y - ghy) + (l.y - gly),
+                                   (h.z - ghz) + (l.z - glz), h.w);
             }
-            list_n = 0;
+            list_n += (int)step_total;
+            if (COUNTED) n_acc += step_total;
             __syncwarp();
         }
-        float4* L = ilist[wi] + list_n + pos;
-        if (mono) L[0] = mono_e;
-        for (uint32_t j = 0; j < d_count; ++j) {
-            const float4 h = sorted4[d_first + j], l = sorted4lo[d_first + j];
-            L[j] = make_float4((h.x - ghx) + (l.x - glx), (h.y - ghy) + (l.y - gly),
-                               (h.z - ghz) + (l.z - glz), h.w);
+        __syncwarp();
+        float fx, fy, fz;
+        flush_list(ilist[wi], list_n, px, py, pz, eps2, fx, fy, fz);
+        if (valid) {
+            ax[me] = ((double)hx + (double)lx) + (double)fx;
+            ay[me] = ((double)hy + (double)ly) + (double)fy;
+            az[me] = ((double)hz + (double)lz) + (double)fz;
         }
-        list_n += (int)step_total;
-        n_acc += step_total;
+        const unsigned valid_lanes = __popc(__ballot_sync(0xffffffffu, valid));
+        if (COUNTED) {
+            t_acc += n_acc * (unsigned long long)valid_lanes;
+            t_mlp += n_mlp;
+            t_cells += n_cells;
+            t_steps += n_steps;
+        }
         __syncwarp();
     }
-    __syncwarp();
-    float fx, fy, fz;
-    flush_list(ilist[wi], list_n, px, py, pz, eps2, fx, fy, fz);
-    if (valid) {
-        ax[me] = ((double)hx + (double)lx) + (double)fx;
-        ay[me] = ((double)hy + (double)ly) + (double)fy;
-        az[me] = ((double)hz + (double)lz) + (double)fz;
-    }
-    const unsigned valid_lanes = __popc(__ballot_sync(0xffffffffu, valid));
-    if (counters && lane == 0) {
-        atomicAdd(&counters[0], n_acc * (unsigned long long)valid_lanes);
-        atomicAdd(&counters[1], n_mlp);
-        atomicAdd(&counters[2], n_cells);
-        atomicAdd(&counters[3], n_steps);
+    if (COUNTED && lane == 0) {
+        atomicAdd(&counters[0], t_acc);
+        atomicAdd(&counters[1], t_mlp);
+        atomicAdd(&counters[2], t_cells);
+        atomicAdd(&counters[3], t_steps);
     }
 }
 
@@ -908,8 +937,11 @@ nb_status nb_mlp_predict(nb_ctx* ctx, const float* params, const float* X, uint3
 }
 
 nb_status nb_bh_set_policy(nb_bh_tree* t, const float* params_dev, float log10_tau,
-                           double theta_fallback, uint32_t count_cap) {
+                           double theta_fallback, uint32_t count_cap, uint32_t flags) {
     if (!t) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_set_policy: null tree");
+    if (flags & ~(uint32_t)NB_POLICY_BOUND_ACCEPT)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_set_policy: unknown flags 0x%x", flags);
+    t->policy_flags = flags;
     t->policy = params_dev;
     t->policy_set = true;
     t->policy_log_tau = log10_tau;
@@ -961,10 +993,16 @@ nb_status launch_learned(nb_ctx* ctx, const nb_bh_tree* t, const double* x, cons
     if (!t->policy_set)
         return set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: NB_OPEN_LEARNED needs nb_bh_set_policy");
     const uint32_t warps = (t->n + 31) / 32;
-    bh_learned_kernel<<<ceil_div(warps, LT_WARPS), LT_THREADS, 0, s>>>(
+    int blocks = ceil_div(warps, LT_WARPS);
+    if (blocks > ctx->sm_count * 4) blocks = ctx->sm_count * 4;  // 4 resident blocks per SM
+    NB_CUDA_TRY(cudaMemsetAsync(t->work, 0, sizeof(uint32_t), s));
+    auto kernel = counters ? bh_learned_kernel<true> : bh_learned_kernel<false>;
+    kernel<<<blocks, LT_THREADS, 0, s>>>(
         t->rec32, t->aux, t->children, t->sorted4, t->sorted4lo, t->n, t->policy,
-        t->policy_log_tau * 0.2f, t->policy_theta * t->policy_theta, t->policy_count_cap,
-        (float)eps2, t->ids, ax, ay, az, counters, ctx->dev_error);
+        t->policy_log_tau * 0.2f,
+        (t->policy_flags & NB_POLICY_BOUND_ACCEPT) ? exp10f(t->policy_log_tau) : 0.f,
+        t->policy_theta * t->policy_theta, t->policy_count_cap,
+        (float)eps2, t->ids, ax, ay, az, counters, ctx->dev_error, t->work);
     return check_launch("bh_learned_kernel");
 }
 

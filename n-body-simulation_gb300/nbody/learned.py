@@ -135,3 +135,111 @@ def timed(fn, reps=3):
     e1.record()
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / reps
+
+
+NO_CAP = 2 ** 31 - 1  # count cap that keeps every cell in the network's range
+
+
+def device_system(d: dict):
+    return {k: _dev(d[k]) for k in ("m", "x", "y", "z", "vx", "vy", "vz")}
+
+
+def training_set(ctx: Context, n: int, n_pairs: int, seeds=(11, 12), theta_gen: float = 0.3,
+                 count_cap: int = NO_CAP, log=None):
+    """Labelled pairs from seeded disc + Plummer mixes of n bodies, n_pairs in total."""
+    import torch
+    Xs, Ys = [], []
+    for s in seeds:
+        d = generators.disc_plummer_mix(n, seed=s)
+        X, Y, found = make_pairs(ctx, d, n_pairs // len(seeds), theta_gen=theta_gen, seed=s,
+                                 count_cap=count_cap)
+        Xs.append(X)
+        Ys.append(Y)
+        if log:
+            log(f"seed {s}: {found} candidate pairs, kept {X.shape[0]}")
+    return torch.cat(Xs), torch.cat(Ys)
+
+
+def sweep(ctx: Context, t: dict, G: float, targets, ref, params, taus, thetas,
+          theta_fallback: float = 0.3, count_cap: int = NO_CAP, eps2: float = EPS2,
+          net_only_taus=()):
+    """Force error (median, p99 over the targets) and time of one traversal for each threshold
+    (learned policy: analytic-bound acceptance, then the network), each theta (the same walk with
+    the group theta rule instead: the method without the network) and each of net_only_taus (the
+    network alone, no bound acceptance). Rows: dict(kind, param, ms, median, p99, interactions,
+    cells, decisions)."""
+    import torch
+    n = t["m"].numel()
+    tree = BHTree(ctx, n, theta=0.5)
+    tree.build(t["m"], t["x"], t["y"], t["z"], G)
+    prev = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    tree.accel(t["x"], t["y"], t["z"], *prev, G, eps2, "group", "f32c")  # |a| of a previous step
+    acc = [torch.zeros_like(v) for v in prev]
+    rows = []
+    cases = ([("theta-walk", th) for th in thetas] + [("learned", lt) for lt in taus]
+             + [("learned-net-only", lt) for lt in net_only_taus])
+    for kind, q in cases:
+        if kind == "theta-walk":
+            tree.set_policy(None, 0.0, q, count_cap)
+        else:
+            tree.set_policy(params, q, theta_fallback, count_cap, bound_accept=(kind == "learned"))
+
+        def run():
+            for a_, b_ in zip(acc, prev):
+                a_.copy_(b_)
+            tree.accel(t["x"], t["y"], t["z"], *acc, G, eps2, "learned", "f32c")
+
+        ms_copy = timed(lambda: [a_.copy_(b_) for a_, b_ in zip(acc, prev)])
+        ms = timed(run) - ms_copy
+        med, p99 = errors(acc, ref, targets)  # acc holds the last run's result
+        for a_, b_ in zip(acc, prev):
+            a_.copy_(b_)
+        inter, dec, cells, _ = tree.accel_learned_counted(t["x"], t["y"], t["z"], *acc, eps2)
+        rows.append({"kind": kind, "param": q, "ms": ms, "median": med, "p99": p99,
+                     "interactions": inter, "cells": cells, "decisions": dec})
+    tree.close()
+    return rows
+
+
+def best_within(rows, kind, median_max=1e-4, p99_max=1e-3, key="ms"):
+    """The row of a kind with the smallest `key` (time, or "interactions") whose error is within
+    both bounds (None if there is none)."""
+    ok = [r for r in rows if r["kind"] == kind and r["median"] <= median_max and r["p99"] <= p99_max]
+    return min(ok, key=lambda r: r[key]) if ok else None
+
+
+def time_steps(ctx: Context, t: dict, G: float, steps: int, opening: str, precision: str,
+               theta: float = 0.5, policy=None, dt: float = 1.0 / 24, eps2: float = EPS2,
+               warmup: int = 3):
+    """ms per leapfrog step (kick + drift, octree build, traversal, kick) of a state copy.
+    policy = (params or None, log10_tau, theta_fallback, count_cap) for opening "learned"."""
+    import torch
+    n = t["m"].numel()
+    pos = [t[k].clone() for k in ("x", "y", "z")]
+    vel = [t[k].clone() for k in ("vx", "vy", "vz")]
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    vh = [torch.zeros_like(a) for a in acc]
+    tree = BHTree(ctx, n, theta=theta)
+    tree.build(t["m"], *pos, G)
+    tree.accel(*pos, *acc, G, eps2, "group", "f32c")  # step 0 accelerations
+    if policy is not None:
+        tree.set_policy(*policy)
+
+    def step():
+        ctx.kick_drift(vh, vel, pos, acc, dt)
+        tree.build(t["m"], *pos, G)
+        tree.accel(*pos, *acc, G, eps2, opening, precision)
+        ctx.kick(vel, vh, acc, dt)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ctx.sync()
+    tree.close()
+    return e0.elapsed_time(e1) / steps

@@ -219,7 +219,7 @@ SIGNATURES.update({
                                                      _vp, _vp, _vp],
     "nb_bh_export_node_ranges": [_vp, _vp, _vp, _vp, _vp],
     "nb_naive_accel_targets": [_vp] + [_vp] * 4 + [_u32, _vp, _u32] + [_vp] * 3 + [_d, _d, _vp],
-    "nb_bh_set_policy": [_vp, _vp, C.c_float, _d, _u32],
+    "nb_bh_set_policy": [_vp, _vp, C.c_float, _d, _u32, _u32],
     "nb_bh_accel_learned_counted": [_vp, _vp] + [_vp] * 6 + [_d, _vp, _vp],
 })
 
@@ -290,10 +290,15 @@ class BHTree:
         check(self.lib.nb_bh_export_node_ranges(self.handle, *[v.ctypes.data for v in a]))
         return {"first": a[0], "count": a[1], "level": a[2], "body": a[3]}
 
-    def set_policy(self, params, log10_tau, theta_fallback=0.5, count_cap=8192):
+    def set_policy(self, params, log10_tau, theta_fallback=0.5, count_cap=8192,
+                   bound_accept=None):
+        """bound_accept (default: on when a network is given) accepts cells whose analytic error
+        bound is below tau before the network is asked."""
         self._policy = params  # keep the device tensor alive
+        if bound_accept is None:
+            bound_accept = params is not None
         check(self.lib.nb_bh_set_policy(self.handle, ptr(params), log10_tau, theta_fallback,
-                                        count_cap))
+                                        count_cap, 1 if bound_accept else 0))
 
     def accel_learned_counted(self, x, y, z, ax, ay, az, eps2, stream=None):
         """NB_OPEN_LEARNED traversal; returns (interactions, policy decisions, cells visited,

@@ -1,0 +1,250 @@
+"""The method's other forms, measured beside the headline Barnes-Hut step (bench.py "also").
+
+* ``precision_form``: naive all-pairs with FP32 pair math and compensated accumulation against
+  the FP64 GPU oracle on a 262,144-body Plummer sphere (G = M = a = 1, softening 1e-3): force
+  error of sampled bodies, pair throughput against the FP32 FMA and SFU (rsqrt) peaks, energy
+  drift over a leapfrog run with dt = 1e-3, and the FP32/FP64 trajectory difference after a few
+  steps.
+* ``batched_ensemble``: 512 independent Plummer spheres with N log-uniform in [256, 16384], FP32
+  forces and FP64 leapfrog, all systems in one persistent pair-kernel launch per step replayed
+  from a captured CUDA graph, tile configuration from the autotuner; against one launch per
+  system.
+* ``learned_form``: learned opening policy on a 50/50 mix of the heliocentric disc and a Plummer
+  sphere (1e-3 Msun, scale radius 0.05 AU, 5 AU from the central body): labelled pairs, training,
+  threshold and theta sweeps at matched error against FP64 naive sums of sampled bodies, and
+  leapfrog steps/s of the learned policy, of the same walk with the theta rule, and of plain
+  per-body theta = 0.5 Barnes-Hut in FP64 (the reference's method).
+
+Every function returns a JSON-ready dict; all compute runs in libnbody_cuda.so.
+"""
+
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+from . import generators, learned
+from .lib import Batch, BHTree, Context, fma_peak
+
+# nominal MUFU rate of one SM (reciprocal square roots per clock) and the GB300's SM count
+# and maximum SM clock: the SFU peak the pair kernels are reported against
+SFU_PER_CLK_PER_SM = 16
+SMS = 152
+SM_MAX_GHZ = 2.07
+
+
+def _events_ms(fn, reps):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _energy(ctx, t, G):
+    import torch
+    out = torch.zeros(4, dtype=torch.float64, device="cuda")
+    ctx.energy(t["m"], t["x"], t["y"], t["z"], t["vx"], t["vy"], t["vz"], G, out)
+    ctx.sync()
+    return out.cpu().tolist()
+
+
+def _leapfrog(ctx, t, acc, vh, G, eps2, dt, steps, precision):
+    pos, vel = [t["x"], t["y"], t["z"]], [t["vx"], t["vy"], t["vz"]]
+    for _ in range(steps):
+        ctx.kick_drift(vh, vel, pos, acc, dt)
+        ctx.naive_accel(t["m"], *pos, *acc, G, eps2, precision)
+        ctx.kick(vel, vh, acc, dt)
+
+
+def precision_form(ctx: Context, n: int = 262144, steps: int = 1000, dt: float = 1e-3,
+                   softening: float = 1e-3, fp64_steps: int = 5, n_targets: int = 4096,
+                   seed: int = 1):
+    import torch
+    d = generators.plummer(n, seed)
+    G, eps2 = 1.0, softening * softening
+    t = learned.device_system(d)
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    targets = learned.sample_targets(n, n_targets)
+    tg = learned._dev(targets.view(np.int32))
+    ref = [torch.zeros(len(targets), dtype=torch.float64, device="cuda") for _ in range(3)]
+    ctx.naive_accel_targets(t["m"], t["x"], t["y"], t["z"], tg, *ref, G, eps2)
+    ctx.sync()
+    ref = [v.cpu().numpy() for v in ref]
+    ms32 = _events_ms(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, G, eps2,
+                                              "f32c"), 5)
+    med, p99 = learned.errors(acc, ref, targets)
+    ms64 = _events_ms(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, G, eps2,
+                                              "f64"), 1)
+    pairs = float(n) * n
+    fp32_peak = fma_peak(ctx, fp64=False)
+    gps32 = pairs / (ms32 * 1e-3)
+    sfu_peak = SFU_PER_CLK_PER_SM * SMS * SM_MAX_GHZ * 1e9
+    # FP32C vs FP64 over a few steps from the same state
+    s32 = {k: v.clone() for k, v in t.items()}
+    s64 = {k: v.clone() for k, v in t.items()}
+    for s, prec in ((s32, "f32c"), (s64, "f64")):
+        a = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+        vh = [torch.zeros_like(v) for v in a]
+        ctx.naive_accel(s["m"], s["x"], s["y"], s["z"], *a, G, eps2, prec)
+        _leapfrog(ctx, s, a, vh, G, eps2, dt, fp64_steps, prec)
+    ctx.sync()
+    dpos = max(float((s32[k] - s64[k]).abs().max()) for k in ("x", "y", "z"))
+    # energy drift of the FP32-force run over `steps` steps
+    e0 = _energy(ctx, t, G)
+    vh = [torch.zeros_like(v) for v in acc]
+    ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, G, eps2, "f32c")
+    t0 = time.perf_counter()
+    _leapfrog(ctx, t, acc, vh, G, eps2, dt, steps, "f32c")
+    ctx.sync()
+    run_s = time.perf_counter() - t0
+    e1 = _energy(ctx, t, G)
+    return {
+        "workload": f"naive all-pairs, {n}-body Plummer sphere (G=M=a=1, seed {seed}), "
+                    f"softening {softening}",
+        "f32c_ms_per_eval": ms32, "f64_ms_per_eval": ms64,
+        "f32c_gpairs_per_s": gps32 / 1e9, "f64_gpairs_per_s": pairs / (ms64 * 1e-3) / 1e9,
+        "f32c_frac_of_measured_fp32_fma_peak": gps32 * 20 / fp32_peak,
+        "fp32_fma_peak_tflops_measured": fp32_peak / 1e12,
+        "f32c_frac_of_nominal_sfu_rsqrt_peak": gps32 / sfu_peak,
+        "force_rel_err_vs_fp64": {"median": med, "p99": p99, "bodies": len(targets)},
+        "energy_drift_f32c": {"steps": steps, "dt": dt, "E0": e0[2], "E1": e1[2],
+                              "rel": abs(e1[2] - e0[2]) / abs(e0[2]), "run_s": run_s},
+        "f32c_vs_f64_max_position_diff": {"steps": fp64_steps, "value": dpos},
+    }
+
+
+def _ensemble_counts(systems: int, lo: int, hi: int, seed: int):
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(math.log(lo), math.log(hi), systems)).astype(np.int64)
+
+
+def batched_ensemble(ctx: Context, systems: int = 512, lo: int = 256, hi: int = 16384,
+                     steps: int = 1000, graph_steps: int = 50, dt: float = 1e-3,
+                     softening: float = 1e-3, per_system_steps: int = 10, seed: int = 3):
+    import torch
+    counts = _ensemble_counts(systems, lo, hi, seed)
+    parts = [generators.plummer(int(c), seed=seed * 100003 + s) for s, c in enumerate(counts)]
+    cat = {k: np.concatenate([p[k] for p in parts]) for k in ("m", "x", "y", "z", "vx", "vy", "vz")}
+    n = len(cat["m"])
+    G, eps2 = 1.0, softening * softening
+    pairs = float(np.sum(counts.astype(np.float64) ** 2))
+    t = learned.device_system(cat)
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    vh = [torch.zeros_like(a) for a in acc]
+    b = Batch(ctx, counts)
+    chosen, ms_cfg = b.autotune(t["m"], t["x"], t["y"], t["z"], *acc, G, eps2, reps=3)
+    info = b.info()
+    ms_accel = _events_ms(lambda: b.accel(t["m"], t["x"], t["y"], t["z"], *acc, G, eps2), 5)
+    # graph of `graph_steps` leapfrog steps, replayed until `steps` steps are done
+    b.accel(t["m"], t["x"], t["y"], t["z"], *acc, G, eps2)
+    g = b.graph(t["m"], [t["x"], t["y"], t["z"]], [t["vx"], t["vy"], t["vz"]], vh, acc, G, eps2,
+                dt, graph_steps)
+    g.launch()  # warm-up replay
+    torch.cuda.synchronize()
+    reps = max(1, steps // graph_steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        g.launch()
+    e1.record()
+    torch.cuda.synchronize()
+    ctx.sync()
+    ms_step_graph = e0.elapsed_time(e1) / (reps * graph_steps)
+    g.close()
+    # one launch per system (FP32C naive on each system's slice), same leapfrog kernels
+    offs = np.concatenate([[0], np.cumsum(counts)])
+    views = [{k: t[k][offs[s]:offs[s + 1]] for k in ("m", "x", "y", "z")} for s in range(systems)]
+    acc_views = [[a[offs[s]:offs[s + 1]] for a in acc] for s in range(systems)]
+
+    def per_system_step():
+        pos, vel = [t["x"], t["y"], t["z"]], [t["vx"], t["vy"], t["vz"]]
+        ctx.kick_drift(vh, vel, pos, acc, dt)
+        for v, a in zip(views, acc_views):
+            ctx.naive_accel(v["m"], v["x"], v["y"], v["z"], *a, G, eps2, "f32c")
+        ctx.kick(vel, vh, acc, dt)
+
+    ms_step_sep = _events_ms(per_system_step, per_system_steps)
+    ctx.sync()
+    b.close()
+    return {
+        "workload": f"{systems} Plummer spheres, N log-uniform in [{lo}, {hi}] (seed {seed}), "
+                    f"{n} bodies, softening {softening}, dt {dt}, FP32C forces + FP64 leapfrog",
+        "pairs_per_step": pairs, "autotune_choice": chosen, "autotune_ms_per_config": ms_cfg,
+        "tile": info,
+        "accel_only_gpairs_per_s": pairs / (ms_accel * 1e-3) / 1e9,
+        "graph": {"steps": reps * graph_steps, "steps_per_graph": graph_steps,
+                  "ms_per_step": ms_step_graph,
+                  "gpairs_per_s": pairs / (ms_step_graph * 1e-3) / 1e9},
+        "one_launch_per_system": {"steps": per_system_steps, "ms_per_step": ms_step_sep,
+                                  "gpairs_per_s": pairs / (ms_step_sep * 1e-3) / 1e9},
+        "graph_speedup": ms_step_sep / ms_step_graph,
+    }
+
+
+def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epochs: int = 4,
+                 steps: int = 20, n_targets: int = 8192, eval_seed: int = 21,
+                 taus=(-4.75, -4.5, -4.25, -4.0, -3.75, -3.5),
+                 thetas=(0.3, 0.35, 0.4, 0.45, 0.5), log=None):
+    import torch
+    t0 = time.perf_counter()
+    X, Y = learned.training_set(ctx, n, n_pairs, log=log)
+    torch.cuda.synchronize()
+    t_pairs = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    params, hist = learned.train(ctx, X, Y, epochs=epochs, batch=8192, lr=2e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    n_train = int(X.shape[0])
+    del X, Y
+    d = generators.disc_plummer_mix(n, seed=eval_seed)
+    t = learned.device_system(d)
+    G = d["G"]
+    targets = learned.sample_targets(n, n_targets)
+    ref = learned.fp64_reference(ctx, t, G, targets)
+    rows = learned.sweep(ctx, t, G, targets, ref, params, taus=taus, thetas=thetas)
+    # plain Barnes-Hut: the reference's per-body rule with theta = 0.5, FP64 (error of one
+    # traversal on the same state)
+    tree = BHTree(ctx, n, theta=0.5)
+    tree.build(t["m"], t["x"], t["y"], t["z"], G)
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    tree.accel(t["x"], t["y"], t["z"], *acc, G, learned.EPS2, "theta", "f64")
+    p_med, p_p99 = learned.errors(acc, ref, targets)
+    tree.close()
+    bl = learned.best_within(rows, "learned")
+    bt = learned.best_within(rows, "theta-walk")
+    ms_plain = learned.time_steps(ctx, t, G, steps, "theta", "f64", theta=0.5)
+    ms_l = (learned.time_steps(ctx, t, G, steps, "learned", "f32c",
+                               policy=(params, bl["param"], 0.3, learned.NO_CAP))
+            if bl else None)
+    ms_t = (learned.time_steps(ctx, t, G, steps, "learned", "f32c",
+                               policy=(None, 0.0, bt["param"], learned.NO_CAP))
+            if bt else None)
+    out = {
+        "workload": f"{n}-body 50/50 heliocentric disc + Plummer sphere (1e-3 Msun, a = 0.05 AU, "
+                    f"5 AU from the central body), evaluation seed {eval_seed}; FP32 forces, FP64 "
+                    f"leapfrog, dt = 1 h",
+        "training": {"pairs": n_train, "pair_generation_s": t_pairs, "epochs": epochs,
+                     "train_s": t_train, "mse_per_epoch": hist},
+        "error_bounds": {"median": 1e-4, "p99": 1e-3, "bodies": len(targets),
+                         "against": "FP64 naive sums (nb_naive_accel_targets)"},
+        "sweep": rows,
+        "plain_theta0.5_fp64": {"median": p_med, "p99": p_p99, "ms_per_step": ms_plain,
+                                "steps_per_s": 1e3 / ms_plain,
+                                "within_bounds": p_med <= 1e-4 and p_p99 <= 1e-3},
+        "learned_best": bl, "theta_walk_best": bt,
+        "learned_ms_per_step": ms_l, "theta_walk_ms_per_step": ms_t,
+    }
+    if ms_l:
+        out["learned_steps_per_s"] = 1e3 / ms_l
+        out["speedup_vs_plain_theta0.5_fp64"] = ms_plain / ms_l
+        if ms_t:
+            out["speedup_vs_theta_walk_matched_error"] = ms_t / ms_l
+    return out

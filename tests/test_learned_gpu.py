@@ -122,3 +122,29 @@ def test_labels_match_cpu_direct_sum(ctx):
             assert abs(Yh[q] - ref) <= 0.05, (q, Yh[q] * 5, ref * 5)
             checked += 1
     assert checked >= 10
+
+
+def test_trained_policy_gain_over_theta_walk(ctx):
+    """What the trained network gains: on a held-out disc + Plummer mix, the learned policy's
+    cheapest setting within 1e-4 median / 1e-3 p99 relative force error (against FP64 naive sums
+    of sampled bodies) needs fewer body-cell interactions than the same walk with the group theta
+    rule at its cheapest setting within the same bounds."""
+    from nbody import generators, learned
+    n = 65536
+    X, Y = learned.training_set(ctx, n, 400_000, seeds=(31, 32))
+    params, hist = learned.train(ctx, X, Y, epochs=3, batch=8192, lr=2e-3)
+    assert hist[-1] < hist[0]
+    d = generators.disc_plummer_mix(n, seed=41)
+    t = learned.device_system(d)
+    targets = learned.sample_targets(n, 4096)
+    ref = learned.fp64_reference(ctx, t, d["G"], targets)
+    rows = learned.sweep(ctx, t, d["G"], targets, ref, params,
+                         taus=(-5.0, -4.75, -4.5, -4.25, -4.0, -3.75, -3.5),
+                         thetas=(0.25, 0.3, 0.35, 0.4, 0.45, 0.5))
+    bl = learned.best_within(rows, "learned", key="interactions")
+    bt = learned.best_within(rows, "theta-walk", key="interactions")
+    assert bl is not None and bt is not None, rows
+    print(f"\nlearned tau 1e{bl['param']}: {bl['interactions'] / n:.0f} interactions/body, "
+          f"p99 {bl['p99']:.2e}, {bl['ms']:.3f} ms; theta-walk {bt['param']}: "
+          f"{bt['interactions'] / n:.0f} interactions/body, p99 {bt['p99']:.2e}, {bt['ms']:.3f} ms")
+    assert bl["interactions"] <= 0.8 * bt["interactions"]
