@@ -92,7 +92,7 @@ nb_status nb_naive_accel_targets(nb_ctx* ctx, const double* m, const double* x, 
 
 /* Tile configuration of the FP32-compensated pair kernel used by nb_naive_accel (process-wide;
  * 0..NB_PAIR_CONFIG_COUNT-1, see nb_batch_info for the shapes; 0 = default). */
-#define NB_PAIR_CONFIG_COUNT 6
+#define NB_PAIR_CONFIG_COUNT 8
 nb_status nb_naive_set_pair_config(int config);
 
 /* ---------------------------------------------------------------------------------------------

@@ -38,17 +38,30 @@ __global__ void plan_single_kernel(uint32_t* sys_off, uint32_t* tgt_begin, uint3
 
 namespace nb {
 
+// (threads, targets per thread, j-tile); X-macro so that the table, the occupancy query and the
+// launch switch list the same instantiations
+#define NB_PAIR_CONFIG_LIST(X)                                                                  \
+    X(0, 128, 12, 256) X(1, 256, 8, 256) X(2, 128, 8, 256) X(3, 64, 8, 256) X(4, 128, 12, 512)      \
+        X(5, 128, 4, 256) X(6, 64, 12, 256) X(7, 128, 8, 128)
+
 const PairConfig kPairConfigs[NB_PAIR_CONFIGS] = {
-    {128, 8, 256}, {128, 4, 256}, {256, 4, 256}, {64, 8, 256}, {128, 8, 128}, {128, 8, 512}};
+#define NB_PAIR_ROW(i, T, IP, JT) {T, IP, JT},
+    NB_PAIR_CONFIG_LIST(NB_PAIR_ROW)
+#undef NB_PAIR_ROW
+};
 
 namespace {
 
-int g_ctas_per_sm[NB_PAIR_CONFIGS] = {0, 0, 0, 0, 0, 0};
+int g_ctas_per_sm[NB_PAIR_CONFIGS] = {};
 
+// Opts the instantiation into its dynamic shared memory and returns its resident CTAs per SM.
 template <int T, int IP, int JT>
-nb_status occupancy(int* out) {
-    NB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, nbpair::pair_f32c_kernel<T, IP, JT>,
-                                                              T, 0));
+nb_status prepare(int* out) {
+    constexpr size_t smem = nbpair::pair_smem_bytes<T, IP, JT>();
+    NB_CUDA_TRY(cudaFuncSetAttribute(nbpair::pair_f32c_kernel<T, IP, JT>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        out, nbpair::pair_f32c_kernel<T, IP, JT>, T, smem));
     if (*out < 1) *out = 1;
     return NB_OK;
 }
@@ -61,8 +74,8 @@ nb_status launch_cfg(const nbpair::Plan& plan, const double* m, const double* x,
     nbpair::pair_prepare_kernel<<<ceil_div(n_total, 256), 256, 0, stream>>>(plan, m, x, y, z, n_total,
                                                                             G, src, tgt);
     NB_TRY(check_launch("pair_prepare_kernel"));
-    nbpair::pair_f32c_kernel<T, IP, JT><<<plan.ctas, T, 0, stream>>>(plan, src, tgt, (float)eps2,
-                                                                     part, err_word);
+    nbpair::pair_f32c_kernel<T, IP, JT><<<plan.ctas, T, nbpair::pair_smem_bytes<T, IP, JT>(),
+                                          stream>>>(plan, src, tgt, (float)eps2, part, err_word);
     NB_TRY(check_launch("pair_f32c_kernel"));
     nbpair::pair_combine_kernel<T * IP, JT><<<ceil_div(n_targets, 256), 256, 0, stream>>>(
         plan, part, n_targets, ax, ay, az);
@@ -71,17 +84,17 @@ nb_status launch_cfg(const nbpair::Plan& plan, const double* m, const double* x,
 
 }  // namespace
 
+// Also makes the configuration launchable (dynamic shared memory opt-in): callers query it
+// before their first launch of a configuration.
 nb_status pair_ctas_per_sm(int cfg, int* out) {
     if (cfg < 0 || cfg >= NB_PAIR_CONFIGS) return set_error(NB_ERR_INVALID_ARG, "bad pair config %d", cfg);
     if (g_ctas_per_sm[cfg] == 0) {
         int v = 0;
         switch (cfg) {
-            case 0: NB_TRY((occupancy<128, 8, 256>(&v))); break;
-            case 1: NB_TRY((occupancy<128, 4, 256>(&v))); break;
-            case 2: NB_TRY((occupancy<256, 4, 256>(&v))); break;
-            case 3: NB_TRY((occupancy<64, 8, 256>(&v))); break;
-            case 4: NB_TRY((occupancy<128, 8, 128>(&v))); break;
-            case 5: NB_TRY((occupancy<128, 8, 512>(&v))); break;
+#define NB_PAIR_PREP(i, T, IP, JT) \
+    case i: NB_TRY((prepare<T, IP, JT>(&v))); break;
+            NB_PAIR_CONFIG_LIST(NB_PAIR_PREP)
+#undef NB_PAIR_PREP
         }
         g_ctas_per_sm[cfg] = v;
     }
@@ -107,13 +120,15 @@ nb_status pair_launch(int cfg, const nbpair::Plan& plan, const double* m, const 
                       double G, double eps2, nbpair::SrcDup* src, float4* tgt, float* part,
                       double* ax, double* ay, double* az, uint32_t* err_word,
                       cudaStream_t stream) {
+    int per_sm = 0;
+    NB_TRY(pair_ctas_per_sm(cfg, &per_sm));  // shared-memory opt-in before the first launch
     switch (cfg) {
-        case 0: return launch_cfg<128, 8, 256>(plan, m, x, y, z, n_total, n_targets, G, eps2, src, tgt, part, ax, ay, az, err_word, stream);
-        case 1: return launch_cfg<128, 4, 256>(plan, m, x, y, z, n_total, n_targets, G, eps2, src, tgt, part, ax, ay, az, err_word, stream);
-        case 2: return launch_cfg<256, 4, 256>(plan, m, x, y, z, n_total, n_targets, G, eps2, src, tgt, part, ax, ay, az, err_word, stream);
-        case 3: return launch_cfg<64, 8, 256>(plan, m, x, y, z, n_total, n_targets, G, eps2, src, tgt, part, ax, ay, az, err_word, stream);
-        case 4: return launch_cfg<128, 8, 128>(plan, m, x, y, z, n_total, n_targets, G, eps2, src, tgt, part, ax, ay, az, err_word, stream);
-        case 5: return launch_cfg<128, 8, 512>(plan, m, x, y, z, n_total, n_targets, G, eps2, src, tgt, part, ax, ay, az, err_word, stream);
+#define NB_PAIR_LAUNCH(i, T, IP, JT)                                                          \
+    case i:                                                                                   \
+        return launch_cfg<T, IP, JT>(plan, m, x, y, z, n_total, n_targets, G, eps2, src, tgt, \
+                                     part, ax, ay, az, err_word, stream);
+        NB_PAIR_CONFIG_LIST(NB_PAIR_LAUNCH)
+#undef NB_PAIR_LAUNCH
         default: return set_error(NB_ERR_INVALID_ARG, "bad pair config %d", cfg);
     }
 }

@@ -11,8 +11,9 @@
 //
 // j-tiles move into shared memory with cp.async.bulk copies that complete on mbarriers (two
 // buffers, every wait bounded: on timeout the CTA sets the timeout bit, drains its in-flight
-// copies with bounded waits and returns). Sources are stored duplicated ({x,x,y,y},{z,z,Gm,Gm})
-// so one broadcast 16-byte shared load feeds packed f32x2 arithmetic on two targets.
+// copies with bounded waits and returns). Source records are 32 bytes ({x,x,y,y},{z,z,Gm,Gm});
+// the scalar inner loop reads them with two broadcast 16-byte shared loads per source (measured
+// faster than a single load of a packed 16-byte {x,y,z,Gm} record).
 #pragma once
 #include "nb_internal.cuh"
 
@@ -108,23 +109,39 @@ __device__ __forceinline__ uint32_t cta_of_unit(const Plan& P, uint64_t u) {
     return c;
 }
 
-#define NB_TWOSUM2(H, L, T)                          \
-    {                                                \
-        const nb_f2 sum_ = f2_add(H, T);             \
-        const nb_f2 bp_ = f2_sub(sum_, H);           \
-        const nb_f2 e1_ = f2_sub(H, f2_sub(sum_, bp_)); \
-        const nb_f2 e2_ = f2_sub(T, bp_);            \
-        L = f2_add(L, f2_add(e1_, e2_));             \
-        H = sum_;                                    \
+// (H, L) += T with Knuth's TwoSum: H + L carries the running sum to about twice FP32 precision.
+#define NB_TWOSUM(H, L, T)                        \
+    {                                             \
+        const float sum_ = (H) + (T);             \
+        const float bp_ = sum_ - (H);             \
+        const float e1_ = (H) - (sum_ - bp_);     \
+        const float e2_ = (T) - bp_;              \
+        (L) = (L) + (e1_ + e2_);                  \
+        (H) = sum_;                               \
     }
 
+// Dynamic shared memory of a configuration: two j-tiles and the per-target (hi, lo) sums.
+template <int THREADS, int IP, int JT>
+constexpr size_t pair_smem_bytes() {
+    return 2 * JT * sizeof(SrcDup) + (size_t)6 * IP * THREADS * sizeof(float);
+}
+
+// Each thread owns IP targets (k-th: i-block * IB + k * THREADS + thread) and walks the j-tile in
+// scalar FP32: per pair 3 subtractions, 3 FMAs for r^2 + eps^2, one MUFU rsqrt, 3 multiplies for
+// G m / r^3 and 3 FMAs into the tile sums, which are added into the compensated (hi, lo) sums
+// once per tile. (Scalar FP32 issues faster here than the packed f32x2 forms of the same
+// arithmetic, which were measured at 83% of its rate.)
 template <int THREADS, int IP, int JT>
 __global__ void __launch_bounds__(THREADS)
 pair_f32c_kernel(Plan P, const SrcDup* __restrict__ src, const float4* __restrict__ tgt,
                  float eps2, float* __restrict__ part, uint32_t* __restrict__ err_word) {
     constexpr int IB = THREADS * IP;
-    constexpr int SLOTS = IP / 2;
-    __shared__ __align__(128) SrcDup tile[2][JT];
+    extern __shared__ __align__(128) unsigned char pair_smem[];
+    SrcDup (*tile)[JT] = reinterpret_cast<SrcDup (*)[JT]>(pair_smem);
+    // compensated per-target sums hl[c][k][thread], c = hx, hy, hz, lx, ly, lz: in shared
+    // memory, since they change once per j-tile and the registers go to more targets per thread
+    float (*hl)[IP][THREADS] =
+        reinterpret_cast<float (*)[IP][THREADS]>(pair_smem + 2 * JT * sizeof(SrcDup));
     __shared__ __align__(8) uint64_t full[2];
 
     const uint32_t cta = blockIdx.x;
@@ -164,13 +181,8 @@ pair_f32c_kernel(Plan P, const SrcDup* __restrict__ src, const float4* __restric
         if (u0 + 1 < u1) issue_next(1);
     }
 
-    const nb_f2 eps2x2 = f2_pack(eps2, eps2);
-    const nb_f2 zero2 = f2_pack(0.f, 0.f);
-    nb_f2 xi[SLOTS], yi[SLOTS], zi[SLOTS];
-    nb_f2 tx[SLOTS], ty[SLOTS], tz[SLOTS];
-    nb_f2 hx[SLOTS], hy[SLOTS], hz[SLOTS];
-    nb_f2 lx[SLOTS], ly[SLOTS], lz[SLOTS];
-
+    const int th = threadIdx.x;
+    float xi[IP], yi[IP], zi[IP], tx[IP], ty[IP], tz[IP];
     uint64_t u = u0;
     uint32_t iter = 0;
     bool failed = false;
@@ -180,16 +192,14 @@ pair_f32c_kernel(Plan P, const SrcDup* __restrict__ src, const float4* __restric
         const uint32_t n_t = P.t_off[w.s + 1] - P.t_off[w.s];
         const uint32_t t0 = w.src0 + P.tgt_begin[w.s];
 #pragma unroll
-        for (int s = 0; s < SLOTS; ++s) {
-            const uint32_t la = w.ib * IB + (2 * s) * THREADS + threadIdx.x;
-            const uint32_t lb = la + THREADS;
-            const float4 a = la < n_t ? tgt[t0 + la] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
-            const float4 b = lb < n_t ? tgt[t0 + lb] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
-            xi[s] = f2_pack(a.x, b.x);
-            yi[s] = f2_pack(a.y, b.y);
-            zi[s] = f2_pack(a.z, b.z);
-            hx[s] = hy[s] = hz[s] = zero2;
-            lx[s] = ly[s] = lz[s] = zero2;
+        for (int k = 0; k < IP; ++k) {
+            const uint32_t li = w.ib * IB + k * THREADS + th;
+            const float4 a = li < n_t ? tgt[t0 + li] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+            xi[k] = a.x;
+            yi[k] = a.y;
+            zi[k] = a.z;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) hl[c][k][th] = 0.f;
         }
         uint32_t jt = w.jt;
         for (; u < seg_end; ++u, ++iter, ++jt) {
@@ -201,36 +211,36 @@ pair_f32c_kernel(Plan P, const SrcDup* __restrict__ src, const float4* __restric
                 break;
             }
 #pragma unroll
-            for (int s = 0; s < SLOTS; ++s) tx[s] = ty[s] = tz[s] = zero2;
-            const ulonglong2* t2 = reinterpret_cast<const ulonglong2*>(&tile[buf][0]);
+            for (int k = 0; k < IP; ++k) tx[k] = ty[k] = tz[k] = 0.f;
+            const float4* t4 = reinterpret_cast<const float4*>(&tile[buf][0]);
 #pragma unroll 2
             for (uint32_t j = 0; j < cnt; ++j) {
-                const ulonglong2 A = t2[2 * j];
-                const ulonglong2 B = t2[2 * j + 1];
+                const float4 A = t4[2 * j], B = t4[2 * j + 1];  // {x,x,y,y}, {z,z,Gm,Gm}
+                const float sx = A.x, sy = A.z, sz = B.x, sm = B.z;
 #pragma unroll
-                for (int s = 0; s < SLOTS; ++s) {
-                    const nb_f2 dx = f2_sub(A.x, xi[s]);
-                    const nb_f2 dy = f2_sub(A.y, yi[s]);
-                    const nb_f2 dz = f2_sub(B.x, zi[s]);
-                    nb_f2 r2 = f2_fma(dx, dx, eps2x2);
-                    r2 = f2_fma(dy, dy, r2);
-                    r2 = f2_fma(dz, dz, r2);
-                    float r2a, r2b;
-                    f2_unpack(r2, r2a, r2b);
-                    const nb_f2 inv = f2_pack(nb_rsqrt_f32(r2a), nb_rsqrt_f32(r2b));
-                    const nb_f2 inv2 = f2_mul(inv, inv);
-                    const nb_f2 mi = f2_mul(B.y, inv);
-                    const nb_f2 s3 = f2_mul(mi, inv2);
-                    tx[s] = f2_fma(dx, s3, tx[s]);
-                    ty[s] = f2_fma(dy, s3, ty[s]);
-                    tz[s] = f2_fma(dz, s3, tz[s]);
+                for (int k = 0; k < IP; ++k) {
+                    const float dx = sx - xi[k], dy = sy - yi[k], dz = sz - zi[k];
+                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+                    const float inv = nb_rsqrt_f32(r2);
+                    const float s3 = (sm * inv) * (inv * inv);
+                    tx[k] = fmaf(dx, s3, tx[k]);
+                    ty[k] = fmaf(dy, s3, ty[k]);
+                    tz[k] = fmaf(dz, s3, tz[k]);
                 }
             }
 #pragma unroll
-            for (int s = 0; s < SLOTS; ++s) {
-                NB_TWOSUM2(hx[s], lx[s], tx[s]);
-                NB_TWOSUM2(hy[s], ly[s], ty[s]);
-                NB_TWOSUM2(hz[s], lz[s], tz[s]);
+            for (int k = 0; k < IP; ++k) {
+                float h0 = hl[0][k][th], h1 = hl[1][k][th], h2 = hl[2][k][th];
+                float l0 = hl[3][k][th], l1 = hl[4][k][th], l2 = hl[5][k][th];
+                NB_TWOSUM(h0, l0, tx[k]);
+                NB_TWOSUM(h1, l1, ty[k]);
+                NB_TWOSUM(h2, l2, tz[k]);
+                hl[0][k][th] = h0;
+                hl[1][k][th] = h1;
+                hl[2][k][th] = h2;
+                hl[3][k][th] = l0;
+                hl[4][k][th] = l1;
+                hl[5][k][th] = l2;
             }
             __syncthreads();
             if (threadIdx.x == 0 && u + 2 < u1) issue_next(buf);  // the cursor is at u + 2
@@ -238,16 +248,9 @@ pair_f32c_kernel(Plan P, const SrcDup* __restrict__ src, const float4* __restric
         if (failed) break;
         float* out = part + (size_t)(cta + P.ib_off[w.s] + w.ib) * 6 * IB;
 #pragma unroll
-        for (int s = 0; s < SLOTS; ++s) {
-            const int la = (2 * s) * THREADS + threadIdx.x, lb = la + THREADS;
-            float a0, b0;
-            f2_unpack(hx[s], a0, b0); out[0 * IB + la] = a0; out[0 * IB + lb] = b0;
-            f2_unpack(hy[s], a0, b0); out[1 * IB + la] = a0; out[1 * IB + lb] = b0;
-            f2_unpack(hz[s], a0, b0); out[2 * IB + la] = a0; out[2 * IB + lb] = b0;
-            f2_unpack(lx[s], a0, b0); out[3 * IB + la] = a0; out[3 * IB + lb] = b0;
-            f2_unpack(ly[s], a0, b0); out[4 * IB + la] = a0; out[4 * IB + lb] = b0;
-            f2_unpack(lz[s], a0, b0); out[5 * IB + la] = a0; out[5 * IB + lb] = b0;
-        }
+        for (int k = 0; k < IP; ++k)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) out[c * IB + k * THREADS + th] = hl[c][k][th];
     }
     if (failed) {
         if (threadIdx.x == 0) atomicOr(err_word, NB_DEVERR_TIMEOUT);
@@ -291,7 +294,7 @@ namespace nb {
 struct PairConfig {
     int threads, ip, jt;
 };
-constexpr int NB_PAIR_CONFIGS = 6;
+constexpr int NB_PAIR_CONFIGS = 8;
 extern const PairConfig kPairConfigs[NB_PAIR_CONFIGS];
 
 // Host-side plan numbers for a configuration.

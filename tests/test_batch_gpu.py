@@ -69,7 +69,7 @@ def test_batch_matches_oracle_per_system(ctx):
         off += n
 
 
-@pytest.mark.parametrize("config", range(6))
+@pytest.mark.parametrize("config", range(8))
 def test_every_configuration(ctx, config):
     from nbody.lib import Batch, set_naive_pair_config
     cat = ensemble(COUNTS, seed=3)
