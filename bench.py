@@ -154,6 +154,49 @@ def cpu_bh_step_seconds(d, sample_fraction: float):
                                                        "traversal_sample_bodies": len(targets)}
 
 
+def cpu_other_configs():
+    """The restated reference (OpenMP, all host cores) on bounded samples of the other
+    configurations, reported beside the GPU figures as baselines."""
+    import numpy as np
+
+    import oracle
+    from nbody import generators
+    out = {"cores": os.cpu_count(), "kind": "port"}
+    # naive FP64, 16,384-body disc: one full evaluation (the reference's CPU-path configuration)
+    d = generators.heliocentric_disc(16384, 1)
+    t0 = time.perf_counter()
+    oracle.naive_accel(d["m"], d["x"], d["y"], d["z"], d["G"], EPS2)
+    t = time.perf_counter() - t0
+    out["naive_f64_disc_16384"] = {"gpairs_per_s": 16384.0 ** 2 / t / 1e9, "s_per_eval": t,
+                                   "sample": "one full evaluation"}
+    # naive FP64, 262,144-body Plummer: 2,048 evenly strided targets against all sources
+    n = 262144
+    p = generators.plummer(n, 1)
+    tg = np.arange(0, n, n // 2048, dtype=np.uint32)
+    t0 = time.perf_counter()
+    oracle.naive_accel_subset(p["m"], p["x"], p["y"], p["z"], tg, 1.0, 1e-6)
+    t = time.perf_counter() - t0
+    out["naive_f64_plummer_262144"] = {"gpairs_per_s": len(tg) * float(n) / t / 1e9,
+                                       "sample": f"{len(tg)} strided targets x {n} sources"}
+    # Barnes-Hut theta = 0.5 on the 1,048,576-body disc + Plummer mix: full build, every 64th
+    # body traversed, scaled to all bodies
+    try:
+        mix = generators.disc_plummer_mix(1 << 20, seed=21)
+        n = len(mix["m"])
+        t0 = time.perf_counter()
+        tree = oracle.build_subtrees(mix["m"], mix["x"], mix["y"], mix["z"], storage_param=32)
+        t1 = time.perf_counter()
+        tg = np.arange(0, n, 64, dtype=np.uint32)
+        oracle.bh_accel_subset(tree, mix["x"], mix["y"], mix["z"], tg, mix["G"], EPS2, THETA)
+        t2 = time.perf_counter()
+        step = (t1 - t0) + (t2 - t1) * n / len(tg)
+        out["bh_theta0.5_mix_1M"] = {"steps_per_s": 1.0 / step, "build_s": t1 - t0,
+                                     "sample": "full build + every 64th body traversed, scaled"}
+    except Exception as e:  # reported, not fatal: the GPU figures do not depend on it
+        out["bh_theta0.5_mix_1M"] = {"error": str(e)}
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -331,6 +374,8 @@ def run_ours(args):
         also = secondary_measurements(ctx, tree, m, pos, acc, G)
 
     cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline and not args.quick:
+        also["cpu_baselines_other_configs"] = cpu_other_configs()
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         t_cpu, parts = cpu_bh_step_seconds(d, 1.0 / 16)
         cpu = {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
