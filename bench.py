@@ -458,6 +458,30 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
         tree.accel(*pos, *acc, G, EPS2, "group", "f32c")
     ms = timed(bh32, 10)
     out["bh_f32c_group_theta0.5_1M"] = {"build_plus_traversal_ms": ms, "steps_per_s": 1e3 / ms}
+    # the headline step with the double-float traversal (NB_DF64: same accepted cells, monopoles
+    # in FP32-pair arithmetic) on a copy of the state, and its force difference to FP64
+    pos2 = [p.clone() for p in pos]
+    acc64 = [a.clone() for a in acc]
+    acc2 = [torch.zeros_like(a) for a in acc]
+    tree.build(m, *pos2, G)
+    tree.accel(*pos2, *acc64, G, EPS2, "theta", "f64")
+    tree.accel(*pos2, *acc2, G, EPS2, "theta", "df64")
+    torch.cuda.synchronize()
+    num = torch.sqrt(sum((u - v) ** 2 for u, v in zip(acc2, acc64)))
+    rel = (num / torch.sqrt(sum(u * u for u in acc64))).cpu()
+
+    def bh_df():
+        tree.build(m, *pos2, G)
+        tree.accel(*pos2, *acc2, G, EPS2, "theta", "df64")
+    ms = timed(bh_df, 10)
+    ms_tr = timed(lambda: tree.accel(*pos2, *acc2, G, EPS2, "theta", "df64"), 10)
+    out["bh_df64_theta0.5_1M"] = {
+        "build_plus_traversal_ms": ms, "traversal_ms": ms_tr,
+        "steps_per_s_excluding_leapfrog": 1e3 / ms,
+        "rel_diff_vs_f64": {"median": float(rel.median()), "p99": float(rel.quantile(0.99)),
+                            "max": float(rel.max())},
+        "arithmetic": "double-float (FP32 pairs, ~2^-46 per pair term) for the accepted "
+                      "monopoles; FP64 for positions, opening decisions and the output"}
     # naive FP64 on the reference's CPU-path configuration (16,384-body disc)
     n = 16384
     dd = generators.heliocentric_disc(n, 1)

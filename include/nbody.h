@@ -49,7 +49,9 @@ typedef enum nb_precision {
     NB_F64_IEEE = 1,  /* FP64, every operation separately and correctly rounded in the reference's
                          order (1/sqrt for sycl::rsqrt): bit-identical to a host FP64 evaluation
                          of the reference's formula */
-    NB_F32C = 2       /* FP32 pair math, compensated (TwoSum) per-body accumulation */
+    NB_F32C = 2,      /* FP32 pair math, compensated (TwoSum) per-body accumulation */
+    NB_DF64 = 3       /* FP64-accurate double-float (pairs of FP32, ~2^-48 per operation) on the
+                         FP32 pipe: Barnes-Hut per-body rule only, same accepted cells as NB_F64 */
 } nb_precision;
 
 #define NB_MAX_TREE_DEPTH 42

@@ -250,6 +250,8 @@ struct ComArgs {
     double *comx, *comy, *comz, *mass, *q;
     NodeRec64* rec64;
     NodeRec32* rec32;
+    float4* rec32lo;
+    float4* rec32lo2;
     NodeAux* aux;
     const uint32_t* node_first_pos;
     uint32_t* children;
@@ -286,6 +288,20 @@ __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double 
     q.body = body;
     q.level = (uint32_t)level;
     A.rec32[idx] = q;
+    // further FP32 terms: the centre minus the box centre, exactly, as a triple-float (rec32,
+    // rec32lo, rec32lo2 .xyz) and G*mass as a double-float (rec32.gm, rec32lo.w)
+    float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), lo2 = lo;
+    if (sm != 0) {
+        const double ox = A.box[0] + A.box[6] / 2, oy = A.box[1] + A.box[6] / 2,
+                     oz = A.box[2] + A.box[6] / 2;
+        float hx, hy, hz;  // equal to q.cx, q.cy, q.cz (both round the same FP64 difference)
+        tf_split_diff(r.cx, ox, hx, lo.x, lo2.x);
+        tf_split_diff(r.cy, oy, hy, lo.y, lo2.y);
+        tf_split_diff(r.cz, oz, hz, lo.z, lo2.z);
+        lo.w = (float)(A.G * sm - (double)q.gm);
+    }
+    A.rec32lo[idx] = lo;
+    A.rec32lo2[idx] = lo2;
     // spread^2 = sum m |x-o|^2 / M - |c-o|^2 (o = box centre, which keeps both terms small)
     NodeAux x;
     if (sm != 0) {
@@ -420,6 +436,8 @@ void carve(nb_bh_tree* t, Carver& c) {
     t->node_mass = c.take<double>(cap);
     t->rec64 = c.take<NodeRec64>(cap);
     t->rec32 = c.take<NodeRec32>(cap);
+    t->rec32lo = c.take<float4>(cap);
+    t->rec32lo2 = c.take<float4>(cap);
     t->node_q = c.take<double>(cap);
     t->aux = c.take<NodeAux>(cap);
     t->children = c.take<uint32_t>(cap * 8);
@@ -556,6 +574,8 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     A.mass = t->node_mass;
     A.rec64 = t->rec64;
     A.rec32 = t->rec32;
+    A.rec32lo = t->rec32lo;
+    A.rec32lo2 = t->rec32lo2;
     A.q = t->node_q;
     A.aux = t->aux;
     A.node_first_pos = t->node_first;

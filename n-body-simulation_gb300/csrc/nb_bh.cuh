@@ -65,6 +65,8 @@ struct nb_bh_tree {
     double *node_comx = nullptr, *node_comy = nullptr, *node_comz = nullptr, *node_mass = nullptr;
     NodeRec64* rec64 = nullptr;
     NodeRec32* rec32 = nullptr;
+    float4* rec32lo = nullptr;   // second FP32 terms of rec32's centre and G*mass
+    float4* rec32lo2 = nullptr;  // third FP32 terms of the centre (triple-float: exact FP64)
     double* node_q = nullptr;  // sum of m |x - box centre|^2 (for the spread)
     NodeAux* aux = nullptr;
     uint32_t* children = nullptr;  // 8 per node: children in visit order, NB_NONE padded

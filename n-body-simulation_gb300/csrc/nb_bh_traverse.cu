@@ -176,6 +176,116 @@ bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __res
     az[me] = A::mul(acz, G);
 }
 
+// Per-body reference rule with FP64-accurate double-float monopoles (NB_DF64). The walk and the
+// opening decisions are those of bh_theta_lane_kernel (FP32 pre-test with a proven margin, the
+// reference's FP64 expression for undecided cells), so each body accepts exactly the reference's
+// cells; the accepted monopoles are evaluated in double-float arithmetic on the FP32 pipe
+// (~2^-48 relative per operation) instead of on the FP64 pipe, which this part runs at 1/64 of
+// the FP32 rate. Centres and the body are exact triple-floats relative to the box centre (rec32,
+// rec32lo, rec32lo2), so the separation is accurate to ~2^-48 of itself; G*mass is rec32.gm +
+// rec32lo.w. rsqrt: hardware estimate y0 plus the third-order step
+// y = y0 (1 + e/2 + 3e^2/8), e = 1 - r^2 y0^2 evaluated with error-free products. The sums are
+// Neumaier-compensated (hi + running lo), converted to FP64 at the end and scaled by G / G_build.
+__global__ void __launch_bounds__(TR_THREADS)
+bh_theta_df_kernel(const NodeRec32* __restrict__ rec32, const float4* __restrict__ rec32lo,
+                   const float4* __restrict__ rec32lo2, const NodeRec64* __restrict__ rec64, const uint32_t* __restrict__ info,
+                   const uint32_t* __restrict__ ids, const double* __restrict__ x,
+                   const double* __restrict__ y, const double* __restrict__ z,
+                   const double* __restrict__ box, uint32_t n, double theta, double eps2,
+                   double gscale, double* __restrict__ ax, double* __restrict__ ay,
+                   double* __restrict__ az) {
+    using A = Arith<FAST64>;
+    const uint32_t p = blockIdx.x * TR_THREADS + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t nn = info[0];
+    const uint32_t me = ids[p];
+    const double px = x[me], py = y[me], pz = z[me];
+    const double E = box[6];
+    const double ox = box[0] + E / 2, oy = box[1] + E / 2, oz = box[2] + E / 2;
+    const float pxf = (float)(px - ox), pyf = (float)(py - oy), pzf = (float)(pz - oz);
+    // the body minus the box centre, exactly, as triple-floats (pxf etc. are their leading terms)
+    float hx, hy, hz, pxm, pym, pzm, pxl, pyl, pzl;
+    tf_split_diff(px, ox, hx, pxm, pxl);
+    tf_split_diff(py, oy, hy, pym, pyl);
+    tf_split_diff(pz, oz, hz, pzm, pzl);
+    const float e2h = (float)eps2, e2l = (float)(eps2 - (double)e2h);
+    const float th2 = (float)(theta * theta);
+    const float u4 = 4.0f * 5.9604645e-8f;  // 4 * 2^-24
+    const float Ef = (float)E;
+    float ahx = 0.f, ahy = 0.f, ahz = 0.f, alx = 0.f, aly = 0.f, alz = 0.f;
+    uint32_t k = 0;
+    while (k < nn) {
+        const NodeRec32 r = rec32[k];
+        if (r.body == me) {
+            k = r.skip;
+            continue;
+        }
+        bool accept = r.body != NB_NONE;
+        if (!accept) {
+            const float dxf = r.cx - pxf, dyf = r.cy - pyf, dzf = r.cz - pzf;
+            const float d2f = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
+            const float t = th2 * d2f;
+            const float rel = u4 * (3.5f * Ef * nb_rsqrt_f32(d2f) + 8.0f);
+            const float margin = t * rel + u4 * r.edge2;
+            if (r.edge2 > t + margin) {
+                accept = false;
+            } else if (r.edge2 < t - margin) {
+                accept = true;
+            } else {
+                const NodeRec64 q = rec64[k];
+                const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py), dz = A::sub(q.cz, pz);
+                accept = A::mul(q.edge, A::rsqrt(A::norm2(dx, dy, dz))) < theta;
+            }
+        }
+        if (accept) {
+            const float4 lo = rec32lo[k];
+            if (r.gm != 0.f || lo.w != 0.f) {
+                const float4 lo2 = rec32lo2[k];
+                const nb_df dx = tf_diff(r.cx, lo.x, lo2.x, pxf, pxm, pxl);
+                const nb_df dy = tf_diff(r.cy, lo.y, lo2.y, pyf, pym, pyl);
+                const nb_df dz = tf_diff(r.cz, lo.z, lo2.z, pzf, pzm, pzl);
+                // r^2 + eps^2
+                const nb_df sx = df_sqr(dx), sy = df_sqr(dy), sz = df_sqr(dz);
+                nb_df a = df_two_sum(sx.h, sy.h);
+                a.l += sx.l + sy.l;
+                nb_df b = df_two_sum(a.h, sz.h);
+                b.l += a.l + sz.l;
+                nb_df c = df_two_sum(b.h, e2h);  // eps^2 may be as large as r^2
+                c.l += b.l + e2l;
+                const nb_df r2 = df_two_sum(c.h, c.l);
+                // 1/r
+                const float y0 = nb_rsqrt_f32(r2.h);
+                const float q = y0 * y0, qe = fmaf(y0, y0, -q);  // y0^2 = q + qe exactly
+                const float th = r2.h * q;
+                float te = fmaf(r2.h, q, -th);
+                te = fmaf(r2.h, qe, te);
+                te = fmaf(r2.l, q, te);
+                const float e = (1.0f - th) - te;  // 1 - th is exact (th is within 2^-21 of 1)
+                const nb_df inv = df_fast_two_sum(y0, y0 * (e * fmaf(0.375f, e, 0.5f)));
+                // G m / r^3
+                const nb_df w = df_mul(nb_df{r.gm, lo.w}, df_mul(df_sqr(inv), inv));
+                // compensated sums
+                const nb_df tx = df_mul(dx, w), ty = df_mul(dy, w), tz = df_mul(dz, w);
+                nb_df s = df_two_sum(ahx, tx.h);
+                ahx = s.h;
+                alx += s.l + tx.l;
+                s = df_two_sum(ahy, ty.h);
+                ahy = s.h;
+                aly += s.l + ty.l;
+                s = df_two_sum(ahz, tz.h);
+                ahz = s.h;
+                alz += s.l + tz.l;
+            }
+            k = r.skip;
+        } else {
+            k = k + 1;
+        }
+    }
+    ax[me] = ((double)ahx + (double)alx) * gscale;
+    ay[me] = ((double)ahy + (double)aly) * gscale;
+    az[me] = ((double)ahz + (double)alz) * gscale;
+}
+
 // Per-body reference rule with FP32 pair math and compensated accumulation.
 __global__ void __launch_bounds__(TR_THREADS)
 bh_theta_f32_kernel(const NodeRec32* __restrict__ rec, const uint32_t* __restrict__ info,
@@ -455,6 +565,13 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
                     t->rec32, t->rec64, t->info, t->ids, x, y, z, t->box, n, theta, eps2, G, ax,
                     ay, az);
                 return nb::check_launch("bh_theta_lane_kernel");
+            case NB_DF64:
+                if (t->G == 0)
+                    return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: NB_DF64 needs a build with G != 0");
+                bh_theta_df_kernel<<<grid, TR_THREADS, 0, s>>>(
+                    t->rec32, t->rec32lo, t->rec32lo2, t->rec64, t->info, t->ids, x, y, z, t->box, n, theta,
+                    eps2, G / t->G, ax, ay, az);
+                return nb::check_launch("bh_theta_df_kernel");
             case NB_F32C:
                 if (G != t->G)
                     return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: G differs from the build's");

@@ -122,3 +122,65 @@ __device__ __forceinline__ nb_f2 f2_fma(nb_f2 a, nb_f2 b, nb_f2 c) {
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
     return d;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Double-float arithmetic: a value is hi + lo with two FP32 numbers, |lo| <= ulp(hi)/2, which
+// carries 48 significant bits (relative rounding ~2^-48 = 3.6e-15 per operation) on the FP32
+// pipe. Error-free transformations after Knuth (TwoSum), Dekker/FMA (TwoProduct); products and
+// sums as in the double-double literature (e.g. Hida, Li, Bailey, "Library for double-double
+// and quad-double arithmetic", 2000), restated for float pairs.
+// ---------------------------------------------------------------------------------------------
+struct nb_df {
+    float h, l;
+};
+// s + e = a + b exactly
+__device__ __forceinline__ nb_df df_two_sum(float a, float b) {
+    const float s = a + b, bb = s - a;
+    return nb_df{s, (a - (s - bb)) + (b - bb)};
+}
+// s + e = a + b exactly, given |a| >= |b| (or a == 0)
+__device__ __forceinline__ nb_df df_fast_two_sum(float a, float b) {
+    const float s = a + b;
+    return nb_df{s, b - (s - a)};
+}
+// a - b
+__device__ __forceinline__ nb_df df_sub(nb_df a, nb_df b) {
+    const nb_df s = df_two_sum(a.h, -b.h);
+    return df_fast_two_sum(s.h, s.l + (a.l - b.l));
+}
+// a * b
+__device__ __forceinline__ nb_df df_mul(nb_df a, nb_df b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return df_fast_two_sum(p, e);
+}
+// a * a
+__device__ __forceinline__ nb_df df_sqr(nb_df a) {
+    const float p = a.h * a.h;
+    float e = fmaf(a.h, a.h, -p);
+    e = fmaf(a.h + a.h, a.l, e);
+    return df_fast_two_sum(p, e);
+}
+// (ch + cm + cl) - (ph + pm + pl) as a double-float, for two triple-float numbers (x = h + m + l
+// with h = fl(x), m = fl(x - h), l = fl(x - h - m): 72 bits, so FP64 values are exact). The two
+// leading differences are error-free, so the result is accurate to ~2^-48 of the difference
+// itself however close the two numbers are.
+__device__ __forceinline__ nb_df tf_diff(float ch, float cm, float cl, float ph, float pm, float pl) {
+    const nb_df s = df_two_sum(ch, -ph);
+    const nb_df t = df_two_sum(cm, -pm);
+    const nb_df u = df_two_sum(s.h, t.h);
+    return df_fast_two_sum(u.h, u.l + (s.l + t.l + (cl - pl)));
+}
+// The exact value of a - b (two FP64 numbers) as a triple-float h + m + l: FP64 TwoSum, then the
+// rounded difference and its error split into FP32 terms.
+__host__ __device__ __forceinline__ void tf_split_diff(double a, double b, float& h, float& m,
+                                                       float& l) {
+    const double s = a - b, bb = s - a;
+    const double err = (a - (s - bb)) + (-b - bb);
+    h = (float)s;
+    const double rem = (s - (double)h) + err;
+    m = (float)rem;
+    l = (float)(rem - (double)m);
+}

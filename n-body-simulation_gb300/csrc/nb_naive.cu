@@ -209,6 +209,8 @@ nb_status naive_dispatch(nb_ctx* ctx, const double* m, const double* x, const do
             return nb::check_launch("naive_f64_kernel");
         case NB_F32C:
             return naive_f32c(ctx, m, x, y, z, ax, ay, az, n, i_begin, i_end, G, eps2, stream);
+        case NB_DF64:
+            return nb::set_error(NB_ERR_UNSUPPORTED, "nb_naive_accel: NB_DF64 is a Barnes-Hut mode");
         default:
             return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_accel: unknown precision %d",
                                  (int)prec);

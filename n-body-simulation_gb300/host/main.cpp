@@ -18,7 +18,7 @@ static void usage() {
                  "  times are <double><h|d|m|y>; options: --theta --block_size --opt_stage"
                  " --energy --sort_bodies --max_level_top_octree --storage_size_param"
                  " --stack_size_param --num_wi_* --wg_size_barnes_hut --use_gpus"
-                 " --G --epsilon2 --precision=<f64|f64_ieee|f32c> --opening=<theta|group>\n";
+                 " --G --epsilon2 --precision=<f64|f64_ieee|f32c|df64> --opening=<theta|group>\n";
 }
 
 static int run(int argc, char** argv) {

@@ -18,8 +18,8 @@ STATUS_NAMES = {0: "NB_OK", 1: "NB_ERR_INVALID_ARG", 2: "NB_ERR_CUDA", 3: "NB_ER
                 4: "NB_ERR_POOL_OVERFLOW", 5: "NB_ERR_DEPTH_OVERFLOW", 6: "NB_ERR_STACK_OVERFLOW",
                 7: "NB_ERR_TIMEOUT", 8: "NB_ERR_UNSUPPORTED", 9: "NB_ERR_NOT_BUILT"}
 
-NB_F64, NB_F64_IEEE, NB_F32C = 0, 1, 2
-PRECISIONS = {"f64": NB_F64, "f64_ieee": NB_F64_IEEE, "f32c": NB_F32C}
+NB_F64, NB_F64_IEEE, NB_F32C, NB_DF64 = 0, 1, 2, 3
+PRECISIONS = {"f64": NB_F64, "f64_ieee": NB_F64_IEEE, "f32c": NB_F32C, "df64": NB_DF64}
 
 _vp = C.c_void_p
 _u32 = C.c_uint32

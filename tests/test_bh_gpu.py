@@ -149,6 +149,17 @@ def test_coincident_bodies_report_depth_overflow(ctx):
 
 
 # -- accelerations ------------------------------------------------------------------------------
+def _check_df64(got, ref, median_rel=1e-12, typical_rel=1e-11):
+    """Per-body error relative to max(|a|, median |a|): a body's own |a| can be a tiny remainder
+    of large cancelling terms, where any arithmetic's error is large relative to |a|."""
+    e = rel_err(*got, *ref)
+    diff = np.sqrt(sum((g - r) ** 2 for g, r in zip(got, ref)))
+    mag = np.sqrt(sum(r * r for r in ref))
+    scale = np.maximum(mag, np.median(mag))
+    assert np.median(e) <= median_rel, np.median(e)
+    assert (diff / scale).max() <= typical_rel, (diff / scale).max()
+
+
 @pytest.mark.parametrize("kind,n,theta", [("disc", 3000, 0.5), ("disc", 3000, 1.05),
                                           ("plummer", 4000, 0.5), ("plummer", 2, 0.5),
                                           ("plummer", 1, 0.5), ("clustered", 2000, 0.7),
@@ -166,6 +177,12 @@ def test_accel_theta_ieee_bit_identical(ctx, kind, n, theta):
     fast = accel(ctx, tree, dd, d["G"], eps2, "theta", "f64")
     if n > 1:
         assert rel_err(*fast, *ref).max() <= 1e-12
+    # double-float monopoles on the FP32 pipe: same accepted cells; each pair term carries
+    # ~2^-46 relative error (FP64: ~2^-52), so the error is bounded against the typical
+    # acceleration, not against a body's own |a| (which can be a tiny remainder of large terms)
+    df = accel(ctx, tree, dd, d["G"], eps2, "theta", "df64")
+    if n > 1:
+        _check_df64(df, ref)
 
 
 def test_theta_zero_equals_direct_sum(ctx):
@@ -174,6 +191,20 @@ def test_theta_zero_equals_direct_sum(ctx):
     got = accel(ctx, tree, dd, 1.0, 1e-6, "theta", "f64")
     ref = oracle.naive_accel(d["m"], d["x"], d["y"], d["z"], 1.0, 1e-6)
     assert rel_err(*got, *ref).max() <= 1e-12
+    _check_df64(accel(ctx, tree, dd, 1.0, 1e-6, "theta", "df64"), ref)
+
+
+def test_df64_matches_f64_on_a_large_disc(ctx):
+    """The headline distribution (disc, masses in kg, G in AU^3 kg^-1 d^-2, eps^2 = 1e-22):
+    double-float monopoles against the FP64 traversal of the same tree."""
+    d = bodies("disc", 100000, seed=23)
+    tree, dd = build(ctx, d, theta=0.5)
+    a64 = accel(ctx, tree, dd, d["G"], 1e-22, "theta", "f64")
+    adf = accel(ctx, tree, dd, d["G"], 1e-22, "theta", "df64")
+    _check_df64(adf, a64)
+    # another G than the build's scales the result
+    adf2 = accel(ctx, tree, dd, 2.0 * d["G"], 1e-22, "theta", "df64")
+    np.testing.assert_allclose(adf2[0], 2.0 * adf[0], rtol=1e-15)
 
 
 @pytest.mark.parametrize("kind,n", [("disc", 20000), ("plummer", 20000)])
