@@ -46,11 +46,7 @@ FLOP_ACCEPTED, FLOP_OPENED = 20, 10
 TRAVERSAL_KERNEL = "bh_theta_lane_kernel"
 
 
-def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+from nbody.replicas import dist_env, job_throughput, max_over_ranks  # noqa: E402
 
 
 class ClockSampler:
@@ -259,13 +255,6 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(v: float) -> float:
-        if dist is None:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
     ctx = Context(local)
     d = generators.heliocentric_disc(N_BODIES, SEED)
     n = N_BODIES
@@ -313,10 +302,10 @@ def run_ours(args):
     barrier()
     clk = clocks.stop()
     ctx.sync()
-    t_total = sum(a.elapsed_time(b) for a, b in step_ms) / 1e3
-    t_total = max_over_ranks(t_total)
+    t_local = sum(a.elapsed_time(b) for a, b in step_ms) / 1e3
+    value = job_throughput(args.steps, t_local, ws, device="cuda")
+    t_total = ws * args.steps / value  # the slowest rank's time
     ms_per_step = t_total / args.steps * 1e3
-    value = ws * args.steps / t_total
     trav_ms = sum(a.elapsed_time(b) for a, b in trav_ev) / len(trav_ev)
 
     # work model of the traversal on the current state
@@ -365,7 +354,7 @@ def run_ours(args):
                           + host_acc, pos + vel + acc):
             hv.copy_(dv, non_blocking=True)
         torch.cuda.synchronize()
-    t_e2e = max_over_ranks(time.perf_counter() - t0)
+    t_e2e = max_over_ranks(time.perf_counter() - t0, device="cuda")
     ctx.sync()
     e2e_value = ws * e2e_steps / t_e2e
 
