@@ -340,7 +340,6 @@ __global__ void com_kernel(ComArgs A) {
     A.sorted4[p] = make_float4(hx, hy, hz, (float)(A.G * mb));
     A.sorted4lo[p] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy),
                                  (float)(rz - (double)hz), 0.f);
-    write_records(A, idx, cx, cy, cz, mb, qb, 1, A.node_level[idx], A.node_skip[idx], b);
     uint32_t cur = A.node_parent[idx];
     while (cur != NB_NONE) {
         __threadfence();
@@ -383,9 +382,18 @@ __global__ void com_kernel(ComArgs A) {
         A.mass[cur] = sm;
         A.q[cur] = sq;
         A.node_count[cur] = count;
-        write_records(A, cur, sx, sy, sz, sm, sq, count, L, end, NB_NONE);
         cur = A.node_parent[cur];
     }
+}
+
+// Traversal records of every node from its sums, one thread per node: the FP64 work (divisions,
+// splits, the spread's square root) runs with full warps here instead of on the few threads
+// that climb the tree in com_kernel.
+__global__ void records_kernel(ComArgs A, const uint32_t* __restrict__ info) {
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= info[0]) return;
+    write_records(A, idx, A.comx[idx], A.comy[idx], A.comz[idx], A.mass[idx], A.q[idx],
+                  A.node_count[idx], A.node_level[idx], A.node_skip[idx], A.node_body[idx]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -584,6 +592,8 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     A.sorted4lo = t->sorted4lo;
     com_kernel<<<grid, BH_THREADS, 0, s>>>(A);
     NB_TRY(nb::check_launch("com_kernel"));
+    records_kernel<<<nb::ceil_div(t->node_cap, BH_THREADS), BH_THREADS, 0, s>>>(A, t->info);
+    NB_TRY(nb::check_launch("records_kernel"));
     t->built = true;
     return NB_OK;
 }
