@@ -314,7 +314,21 @@ def run_ours(args):
     fp64_peak = fma_peak(ctx, fp64=True)
     stats = tree.stats()
 
-    # build passes against HBM: algorithmic bytes of AABB + keys + sort + cells + centre of mass
+    # build passes against HBM, per phase (CUDA events between the phases of nb_bh_build):
+    # algorithmic bytes per body / per node of each phase
+    nodes = stats["node_count"]
+    phase_bytes = {
+        "aabb": 24 * n,                                  # read x, y, z
+        "keys": 24 * n + 12 * n,                         # read x, y, z; write key + id
+        "sort": 8 * 24 * n,                              # 8 radix passes: read + write key + id
+        "cells": 16 * n + 29 * n + 12 * n + 8 * n + 24 * nodes,  # runs, splits, counts, scan,
+                                                         # emit (node level/first/last/skip/...)
+        "centre_of_mass": 64 * n + 305 * nodes,          # body sums + sorted records; per node:
+                                                         # child sums read, sums, child list and
+                                                         # traversal records written
+    }
+    tree.set_phase_timing(True)
+    phase_runs = []
     build_ev = []
     for _ in range(3):
         flush.zero_()
@@ -323,17 +337,12 @@ def run_ours(args):
         tree.build(m, *pos, G)
         b1.record()
         build_ev.append((b0, b1))
+        phase_runs.append(tree.build_phase_ms())
+    tree.set_phase_timing(False)
     torch.cuda.synchronize()
     build_ms = min(a.elapsed_time(b) for a, b in build_ev)
-    nodes = stats["node_count"]
-    build_bytes = (24 * n            # AABB reads x,y,z
-                   + 24 * n + 12 * n  # keys: read x,y,z; write key + id
-                   + 8 * 24 * n       # 8 radix passes: read + write key + id
-                   + 16 * n + 13 * n  # splits: read keys; write level, start, end (+mask)
-                   + 12 * n           # counts + scan
-                   + 24 * nodes       # emit: node level/first/last/skip/parent/body
-                   + 32 * n           # centre of mass: m, x, y, z per body
-                   + (68 + 80) * nodes)  # cell sums read/written + traversal records
+    phase_ms = [min(r[k] for r in phase_runs) for k in range(5)]
+    build_bytes = sum(phase_bytes.values())
     hbm_peak, hbm_src = measured_hbm_peak()
 
     # e2e: same step through the C ABI with the state in pinned host memory
@@ -403,7 +412,12 @@ def run_ours(args):
                                "frac": build_bytes / (build_ms * 1e-3) / 1e9 / hbm_peak,
                                "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
                                "ms_per_build": build_ms, "algorithmic_bytes": build_bytes,
-                               "traffic": load_traffic("bh_build")[0]},
+                               "traffic": load_traffic("bh_build")[0],
+                               "phases": {name: {"ms": ms, "algorithmic_bytes": b,
+                                                 "gbs": b / (ms * 1e-3) / 1e9,
+                                                 "frac": b / (ms * 1e-3) / 1e9 / hbm_peak}
+                                          for (name, b), ms in zip(phase_bytes.items(),
+                                                                   phase_ms)}},
             "tree": {"nodes": nodes, "max_depth": stats["max_depth"],
                      "reference_layout_nodes": stats["ref_node_count"]},
             "clocks": clk,

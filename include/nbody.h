@@ -261,6 +261,12 @@ nb_status nb_bh_tree_set_theta(nb_bh_tree* tree, double theta);
 nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* tree, const double* m, const double* x,
                       const double* y, const double* z, uint32_t n, double G,
                       nb_stream_t stream);
+/* Phase timing of nb_bh_build (for measurements): when enabled, each build records CUDA events at
+ * its phase boundaries; nb_bh_build_phase_ms (synchronous) returns the last build's durations
+ * in ms: [0] AABB, [1] keys, [2] radix sort, [3] cells (runs, splits, counts, scan, emit),
+ * [4] centre of mass and node records. */
+nb_status nb_bh_set_phase_timing(nb_bh_tree* tree, int enable);
+nb_status nb_bh_build_phase_ms(nb_bh_tree* tree, float* ms5);
 
 /* Replaces BarnesHutAlgorithm::computeAccelerations (BarnesHutAlgorithm.hpp:43-46,
  * BarnesHutAlgorithm.cpp:280-401) for the bodies of the last build (same x, y, z). */

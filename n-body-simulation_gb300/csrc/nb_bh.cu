@@ -186,6 +186,12 @@ __device__ __forceinline__ uint32_t parent_of(uint32_t a, uint32_t b, int dl, in
     return node_index(base, mask, split_start[s], split_level[s]);
 }
 
+__device__ __forceinline__ uint32_t digit_at(const uint64_t* __restrict__ key0,
+                                             const uint64_t* __restrict__ key1, uint32_t q, int L) {
+    if (L < NB_KEY_LEVELS) return (uint32_t)(key0[q] >> (60 - 3 * L)) & 7u;
+    return (uint32_t)(key1[q] >> (60 - 3 * (L - NB_KEY_LEVELS))) & 7u;
+}
+
 __global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
                             const uint8_t* __restrict__ split_level,
                             const uint32_t* __restrict__ split_start,
@@ -195,7 +201,8 @@ __global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
                             uint32_t* __restrict__ node_first, uint32_t* __restrict__ node_last,
                             uint32_t* __restrict__ node_skip, uint32_t* __restrict__ node_parent,
                             uint32_t* __restrict__ node_body, uint32_t* __restrict__ node_nchild,
-                            uint32_t* __restrict__ info) {
+                            uint32_t* __restrict__ info, const uint64_t* __restrict__ key0,
+                            const uint64_t* __restrict__ key1, uint32_t* __restrict__ children) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     if (p == 0) info[0] = base[n];
@@ -210,7 +217,11 @@ __global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
         node_body[idx] = ids[p];
         const uint32_t par = parent_of(p, p, dl, dr, split_level, split_start, base, mask);
         node_parent[idx] = par;
-        if (par != NB_NONE) atomicAdd(&node_nchild[par], 1u);
+        if (par != NB_NONE) {
+            atomicAdd(&node_nchild[par], 1u);
+            // the parent's level is the deeper boundary split; slot = visit rank there
+            children[(size_t)par * 8 + digit_at(key0, key1, p, max(dl, dr))] = idx;
+        }
     }
     if (p + 1 < n && split_end[p] != NB_NONE) {  // internal cell whose first split is p
         const uint32_t a = split_start[p], b = split_end[p];
@@ -225,14 +236,11 @@ __global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
         const int dr = b + 1 < n ? (int)split_level[b] : -1;
         const uint32_t par = parent_of(a, b, dl, dr, split_level, split_start, base, mask);
         node_parent[idx] = par;
-        if (par != NB_NONE) atomicAdd(&node_nchild[par], 1u);
+        if (par != NB_NONE) {
+            atomicAdd(&node_nchild[par], 1u);
+            children[(size_t)par * 8 + digit_at(key0, key1, a, max(dl, dr))] = idx;
+        }
     }
-}
-
-__device__ __forceinline__ uint32_t digit_at(const uint64_t* __restrict__ key0,
-                                             const uint64_t* __restrict__ key1, uint32_t q, int L) {
-    if (L < NB_KEY_LEVELS) return (uint32_t)(key0[q] >> (60 - 3 * L)) & 7u;
-    return (uint32_t)(key1[q] >> (60 - 3 * (L - NB_KEY_LEVELS))) & 7u;
 }
 
 struct ComArgs {
@@ -345,29 +353,25 @@ __global__ void com_kernel(ComArgs A) {
         __threadfence();
         if (atomicAdd(&A.node_arrive[cur], 1u) != A.node_nchild[cur] - 1u) return;
         __threadfence();
-        const int L = A.node_level[cur];
-        uint32_t slot[8];
-#pragma unroll
-        for (int o = 0; o < 8; ++o) slot[o] = NB_NONE;
-        const uint32_t end = A.node_skip[cur];
-        uint32_t c = cur + 1;
+        // children by visit rank (written by emit_kernel); rewritten below as the compacted
+        // visit-order list the learned traversal reads
+        uint4* cl = reinterpret_cast<uint4*>(A.children + (size_t)cur * 8);
+        const uint4 c0 = __ldcg(cl), c1 = __ldcg(cl + 1);
+        const uint32_t vs[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
         uint32_t list[8];
         int nch = 0;
-        for (int k = 0; k < 8 && c < end; ++k) {
-            slot[nb_octant_of_visit(digit_at(A.key0, A.key1, A.node_first[c], L))] = c;
-            list[nch++] = c;
-            c = A.node_skip[c];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            list[t] = NB_NONE;
+            if (vs[t] != NB_NONE) list[nch++] = vs[t];
         }
-        uint4* out = reinterpret_cast<uint4*>(A.children + (size_t)cur * 8);
-        out[0] = make_uint4(list[0], nch > 1 ? list[1] : NB_NONE, nch > 2 ? list[2] : NB_NONE,
-                            nch > 3 ? list[3] : NB_NONE);
-        out[1] = make_uint4(nch > 4 ? list[4] : NB_NONE, nch > 5 ? list[5] : NB_NONE,
-                            nch > 6 ? list[6] : NB_NONE, nch > 7 ? list[7] : NB_NONE);
+        cl[0] = make_uint4(list[0], list[1], list[2], list[3]);
+        cl[1] = make_uint4(list[4], list[5], list[6], list[7]);
         double sx = 0, sy = 0, sz = 0, sm = 0, sq = 0;
         uint32_t count = 0;
 #pragma unroll
-        for (int o = 0; o < 8; ++o) {
-            const uint32_t ch = slot[o];
+        for (int o = 0; o < 8; ++o) {  // the reference's octant order 0..7
+            const uint32_t ch = vs[nb_visit_of_octant(o)];
             if (ch == NB_NONE) continue;
             sx = __dadd_rn(sx, __ldcg(&A.comx[ch]));
             sy = __dadd_rn(sy, __ldcg(&A.comy[ch]));
@@ -500,8 +504,36 @@ nb_status nb_bh_tree_create(nb_ctx* ctx, uint32_t n_max, const nb_bh_params* par
 
 nb_status nb_bh_tree_destroy(nb_bh_tree* t) {
     if (!t) return NB_OK;
+    if (t->phase_timing)
+        for (auto& e : t->phase_ev) cudaEventDestroy(e);
     if (t->box) cudaFree(t->box);
     delete t;
+    return NB_OK;
+}
+
+nb_status nb_bh_set_phase_timing(nb_bh_tree* t, int enable) {
+    if (!t) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_set_phase_timing: null tree");
+    NB_CUDA_TRY(cudaSetDevice(t->device));
+    if (enable && !t->phase_timing) {
+        for (auto& e : t->phase_ev) NB_CUDA_TRY(cudaEventCreate(&e));
+    } else if (!enable && t->phase_timing) {
+        for (auto& e : t->phase_ev) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    }
+    t->phase_timing = enable != 0;
+    return NB_OK;
+}
+
+nb_status nb_bh_build_phase_ms(nb_bh_tree* t, float* ms) {
+    if (!t || !ms) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_build_phase_ms: null argument");
+    if (!t->phase_timing)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_build_phase_ms: phase timing is off");
+    if (!t->built) return nb::set_error(NB_ERR_NOT_BUILT, "nb_bh_build_phase_ms: tree not built");
+    NB_CUDA_TRY(cudaEventSynchronize(t->phase_ev[5]));
+    for (int k = 0; k < 5; ++k)
+        NB_CUDA_TRY(cudaEventElapsedTime(&ms[k], t->phase_ev[k], t->phase_ev[k + 1]));
     return NB_OK;
 }
 
@@ -525,9 +557,16 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     t->n = n;
     t->G = G;
     const int grid = nb::ceil_div(n, BH_THREADS);
+    auto mark = [&](int phase) -> nb_status {
+        if (t->phase_timing) NB_CUDA_TRY(cudaEventRecord(t->phase_ev[phase], s));
+        return NB_OK;
+    };
+    NB_TRY(mark(0));
     NB_TRY(nb::launch_aabb(ctx, x, y, z, n, t->box, s));
+    NB_TRY(mark(1));
     keys_kernel<<<grid, BH_THREADS, 0, s>>>(x, y, z, n, t->box, t->key0, t->ids);
     NB_TRY(nb::check_launch("keys_kernel"));
+    NB_TRY(mark(2));
     int in_alt = 0;
     NB_TRY(nb::radix_sort_pairs(t->key0, t->ids, t->key_alt, t->ids_alt, n, 0, 3 * NB_KEY_LEVELS,
                                 t->sort_temp, s, &in_alt));
@@ -535,6 +574,7 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
         NB_CUDA_TRY(cudaMemcpyAsync(t->key0, t->key_alt, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
         NB_CUDA_TRY(cudaMemcpyAsync(t->ids, t->ids_alt, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
     }
+    NB_TRY(mark(3));
     NB_CUDA_TRY(cudaMemsetAsync(t->key1, 0, (size_t)n * 8, s));
     runs_fixup_kernel<<<grid, BH_THREADS, 0, s>>>(x, y, z, n, t->box, t->key0, t->key1, t->ids,
                                                   ctx->dev_error);
@@ -550,11 +590,14 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     const size_t nodes_max = 2 * (size_t)n;
     NB_CUDA_TRY(cudaMemsetAsync(t->node_nchild, 0, nodes_max * 4, s));
     NB_CUDA_TRY(cudaMemsetAsync(t->node_arrive, 0, nodes_max * 4, s));
+    NB_CUDA_TRY(cudaMemsetAsync(t->children, 0xff, nodes_max * 8 * 4, s));  // NB_NONE
     emit_kernel<<<grid, BH_THREADS, 0, s>>>(n, t->ids, t->split_level, t->split_start, t->split_end,
                                             (const unsigned long long*)t->mask, t->base,
                                             t->node_level, t->node_first, t->node_last, t->node_skip,
-                                            t->node_parent, t->node_body, t->node_nchild, t->info);
+                                            t->node_parent, t->node_body, t->node_nchild, t->info,
+                                            t->key0, t->key1, t->children);
     NB_TRY(nb::check_launch("emit_kernel"));
+    NB_TRY(mark(4));
     ComArgs A;
     A.n = n;
     A.m = m;
@@ -594,6 +637,7 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     NB_TRY(nb::check_launch("com_kernel"));
     records_kernel<<<nb::ceil_div(t->node_cap, BH_THREADS), BH_THREADS, 0, s>>>(A, t->info);
     NB_TRY(nb::check_launch("records_kernel"));
+    NB_TRY(mark(5));
     t->built = true;
     return NB_OK;
 }

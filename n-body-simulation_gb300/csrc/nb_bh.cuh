@@ -48,6 +48,8 @@ struct nb_bh_tree {
     double* box = nullptr;  // [0..6] AABB (min xyz, max xyz, edge), [7..9] box centre
     uint32_t* info = nullptr;  // [0] node count (copy of base[n])
     uint32_t* work = nullptr;  // work counter of persistent traversal kernels
+    cudaEvent_t phase_ev[6] = {};  // build phase boundaries (nb_bh_set_phase_timing)
+    bool phase_timing = false;
 
     uint64_t *key0 = nullptr, *key1 = nullptr, *key_alt = nullptr;
     uint32_t *ids = nullptr, *ids_alt = nullptr;

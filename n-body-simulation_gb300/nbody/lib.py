@@ -220,6 +220,8 @@ SIGNATURES.update({
     "nb_bh_export_node_ranges": [_vp, _vp, _vp, _vp, _vp],
     "nb_naive_accel_targets": [_vp] + [_vp] * 4 + [_u32, _vp, _u32] + [_vp] * 3 + [_d, _d, _vp],
     "nb_bh_set_policy": [_vp, _vp, C.c_float, _d, _u32, _u32],
+    "nb_bh_set_phase_timing": [_vp, _i],
+    "nb_bh_build_phase_ms": [_vp, _vp],
     "nb_bh_accel_learned_counted": [_vp, _vp] + [_vp] * 6 + [_d, _vp, _vp],
 })
 
@@ -260,6 +262,15 @@ class BHTree:
     def build(self, m, x, y, z, G, stream=None):
         check(self.lib.nb_bh_build(self.ctx.handle, self.handle, ptr(m), ptr(x), ptr(y), ptr(z),
                                    m.numel(), G, stream_ptr(stream)))
+
+    def set_phase_timing(self, enable=True):
+        check(self.lib.nb_bh_set_phase_timing(self.handle, 1 if enable else 0))
+
+    def build_phase_ms(self):
+        """Durations (ms) of the last build's phases: AABB, keys, sort, cells, centre of mass."""
+        ms = (C.c_float * 5)()
+        check(self.lib.nb_bh_build_phase_ms(self.handle, ms))
+        return list(ms)
 
     def accel(self, x, y, z, ax, ay, az, G, eps2, opening="theta", precision="f64", stream=None):
         check(self.lib.nb_bh_accel(self.ctx.handle, self.handle, ptr(x), ptr(y), ptr(z), ptr(ax),

@@ -248,3 +248,20 @@ def test_lane_and_lockstep_schedules_agree_bitwise(ctx, precision):
     b = accel(ctx, tree, dd, d["G"], 1e-22, "theta", precision)
     for u, v in zip(a, b):
         np.testing.assert_array_equal(u, v)
+
+
+def test_build_phase_timing(ctx):
+    import torch
+    d = bodies("disc", 50000, seed=3)
+    tree, dd = build(ctx, d, theta=0.5)
+    tree.set_phase_timing(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    tree.build(dd["m"], dd["x"], dd["y"], dd["z"], d["G"])
+    e1.record()
+    ms = tree.build_phase_ms()
+    ctx.sync()
+    total = e0.elapsed_time(e1)
+    assert len(ms) == 5 and all(v > 0 for v in ms)
+    assert sum(ms) <= total * 1.05 + 0.05
+    tree.set_phase_timing(False)
