@@ -63,9 +63,7 @@ struct Arith<FAST64> {
     __device__ static double accum(double acc, double m, double d, double inv) {
         return fma(m * inv, d, acc);
     }
-    // m (d2 + eps2)^(-3/2) from the hardware estimate y0 of (d2 + eps2)^(-1/2) with one
-    // correction: (1 - e)^(-3/2) = 1 + 3e/2 + 15e^2/8 + O(e^3), e = 1 - den y0^2 (|e| < 2^-21,
-    // so the dropped terms are below 2^-62): 7 FP64 operations instead of cubing den and
+    // m (d2 + eps2)^(-3/2) by nb_m_rinv3_f64: 7 FP64 operations instead of cubing den and
     // refining its rsqrt (8).
     __device__ static void monopole(double m, double dx, double dy, double dz, double d2,
                                     double eps2, double& ax, double& ay, double& az) {
@@ -77,13 +75,7 @@ struct Arith<FAST64> {
     }
     __device__ static void monopole_den(double m, double dx, double dy, double dz, double den,
                                         double& ax, double& ay, double& az) {
-        double y0;
-        asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y0) : "d"(den));
-        const double y2 = y0 * y0;
-        const double e = fma(-den, y2, 1.0);
-        const double p = fma(1.875, e, 1.5);
-        const double w0 = m * (y2 * y0);
-        const double w = fma(w0 * e, p, w0);
+        const double w = nb_m_rinv3_f64(m, den);
         ax = fma(w, dx, ax);
         ay = fma(w, dy, ay);
         az = fma(w, dz, az);
@@ -405,8 +397,7 @@ bh_group_f64_kernel(const NodeRec64* __restrict__ rec, const uint32_t* __restric
             continue;
         }
         if (valid && r.body != me && r.mass != 0) {
-            const double inv = nb_rsqrt_f64(d2 + eps2);
-            const double s = r.mass * inv * inv * inv;
+            const double s = nb_m_rinv3_f64(r.mass, d2 + eps2);
             acx = fma(s, dx, acx);
             acy = fma(s, dy, acy);
             acz = fma(s, dz, acz);

@@ -85,6 +85,19 @@ __device__ __forceinline__ double nb_rsqrt_f64(double x) {
     return fma(u, p, y0);
 }
 
+// m * den^(-3/2) in FP64: hardware estimate y0 of den^(-1/2) and one correction of its cube,
+// (1 - e)^(-3/2) = 1 + 3e/2 + 15e^2/8 + O(e^3) with e = 1 - den y0^2 (|e| < 2^-21, dropped terms
+// below 2^-62): 7 FP64 operations.
+__device__ __forceinline__ double nb_m_rinv3_f64(double m, double den) {
+    double y0;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y0) : "d"(den));
+    const double y2 = y0 * y0;
+    const double e = fma(-den, y2, 1.0);
+    const double p = fma(1.875, e, 1.5);
+    const double w0 = m * (y2 * y0);
+    return fma(w0 * e, p, w0);
+}
+
 // FP32 reciprocal square root (MUFU.RSQ, ~2 ulp).
 __device__ __forceinline__ float nb_rsqrt_f32(float x) {
     float y;

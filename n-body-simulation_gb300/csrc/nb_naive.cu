@@ -5,8 +5,9 @@
 //    operation separately rounded in the reference's order (r^2 summed left to right, den^3 as
 //    (den*den)*den, 1/sqrt for rsqrt, acc += m*(r*den), G last). Bit-identical to the host
 //    FP64 evaluation of NaiveAlgorithm.cpp:331-351.
-//  * NB_F64: same loop with FMAs and the refined hardware rsqrt (FP64-pipe bound on GB300).
-//  * NB_F32C: the FP32-compensated pair kernel of nb_pair.cuh (packed f32x2 arithmetic, TwoSum
+//  * NB_F64: same loop with FMAs and m (r^2 + eps^2)^(-3/2) from the hardware rsqrt estimate with
+//    one correction (nb_m_rinv3_f64; FP64-pipe bound on GB300).
+//  * NB_F32C: the FP32-compensated pair kernel of nb_pair.cuh (scalar FP32 pair math, TwoSum
 //    accumulation, stream-K persistent CTAs, cp.async.bulk j-tiles behind bounded mbarrier
 //    waits), run as a batch of one system.
 #include "nb_internal.cuh"
@@ -66,10 +67,8 @@ naive_f64_kernel(const double* __restrict__ m, const double* __restrict__ x,
                     const double r_x = sx[jj] - px;
                     const double r_y = sy[jj] - py;
                     const double r_z = sz[jj] - pz;
-                    double den = fma(r_x, r_x, fma(r_y, r_y, fma(r_z, r_z, eps2)));
-                    den = den * den * den;
-                    const double inv = nb_rsqrt_f64(den);
-                    const double s = sm[jj] * inv;
+                    const double den = fma(r_x, r_x, fma(r_y, r_y, fma(r_z, r_z, eps2)));
+                    const double s = nb_m_rinv3_f64(sm[jj], den);
                     acc_x = fma(s, r_x, acc_x);
                     acc_y = fma(s, r_y, acc_y);
                     acc_z = fma(s, r_z, acc_z);
@@ -118,9 +117,8 @@ naive_f64_targets_kernel(const double* __restrict__ m, const double* __restrict_
 #pragma unroll 4
             for (uint32_t jj = 0; jj < cnt; ++jj) {
                 const double r_x = sx[jj] - px, r_y = sy[jj] - py, r_z = sz[jj] - pz;
-                double den = fma(r_x, r_x, fma(r_y, r_y, fma(r_z, r_z, eps2)));
-                den = den * den * den;
-                const double s = sm[jj] * nb_rsqrt_f64(den);
+                const double den = fma(r_x, r_x, fma(r_y, r_y, fma(r_z, r_z, eps2)));
+                const double s = nb_m_rinv3_f64(sm[jj], den);
                 acc_x = fma(s, r_x, acc_x);
                 acc_y = fma(s, r_y, acc_y);
                 acc_z = fma(s, r_z, acc_z);
