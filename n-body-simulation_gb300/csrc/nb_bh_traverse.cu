@@ -146,10 +146,10 @@ bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __res
                      double* __restrict__ ay, double* __restrict__ az) {
     using A = Arith<MODE>;
     const uint32_t p = blockIdx.x * TR_THREADS + threadIdx.x;
-    if (p >= n) return;
+    const bool valid = p < n;  // lanes past the end stay (they take part in the warp votes)
     const uint32_t nn = info[0];
-    const uint32_t me = ids[p];
-    const double px = x[me], py = y[me], pz = z[me];
+    const uint32_t me = valid ? ids[p] : NB_NONE;
+    const double px = valid ? x[me] : 0.0, py = valid ? y[me] : 0.0, pz = valid ? z[me] : 0.0;
     const double E = box[6];
     const double ox = box[0] + E / 2, oy = box[1] + E / 2, oz = box[2] + E / 2;
     const float pxf = (float)(px - ox), pyf = (float)(py - oy), pzf = (float)(pz - oz);
@@ -157,44 +157,59 @@ bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __res
     const float u4 = 4.0f * 5.9604645e-8f;  // 4 * 2^-24
     const float Ef = (float)E;
     double acx = 0, acy = 0, acz = 0;
-    uint32_t k = 0;
-    while (k < nn) {
-        const NodeRec32 r = rec32[k];
-        if (r.body == me) {
-            k = r.skip;
-            continue;
-        }
-        bool accept = r.body != NB_NONE;
-        if (!accept) {
-            const float dxf = r.cx - pxf, dyf = r.cy - pyf, dzf = r.cz - pzf;
-            const float d2f = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
-            const float t = th2 * d2f;
-            const float rel = u4 * (3.5f * Ef * nb_rsqrt_f32(d2f) + 8.0f);
-            const float margin = t * rel + u4 * r.edge2;
-            if (r.edge2 > t + margin) {
-                accept = false;  // certainly opened
-            } else if (r.edge2 < t - margin) {
-                accept = true;   // certainly accepted
-            } else {             // undecided: the reference's FP64 expression
-                const NodeRec64 q = rec64[k];
-                const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py), dz = A::sub(q.cz, pz);
-                accept = A::mul(q.edge, A::rsqrt(A::norm2(dx, dy, dz))) < theta;
+    uint32_t k = valid ? 0u : nn;
+    // Find, then compute: every lane walks (FP32 tests, divergent but off the FP64 pipe) to its
+    // next accepted cell, then the lanes evaluate their FP64 monopoles together, so the FP64
+    // work runs with all unfinished lanes instead of the few that accept in the same iteration.
+    for (;;) {
+        bool found = false;
+        uint32_t next = 0;
+        while (k < nn) {
+            const NodeRec32 r = rec32[k];
+            if (r.body == me) {
+                k = r.skip;
+                continue;
             }
+            bool accept = r.body != NB_NONE;
+            if (!accept) {
+                const float dxf = r.cx - pxf, dyf = r.cy - pyf, dzf = r.cz - pzf;
+                const float d2f = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
+                const float t = th2 * d2f;
+                const float rel = u4 * (3.5f * Ef * nb_rsqrt_f32(d2f) + 8.0f);
+                const float margin = t * rel + u4 * r.edge2;
+                if (r.edge2 > t + margin) {
+                    accept = false;  // certainly opened
+                } else if (r.edge2 < t - margin) {
+                    accept = true;   // certainly accepted
+                } else {             // undecided: the reference's FP64 expression
+                    const NodeRec64 q = rec64[k];
+                    const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py),
+                                 dz = A::sub(q.cz, pz);
+                    accept = A::mul(q.edge, A::rsqrt(A::norm2(dx, dy, dz))) < theta;
+                }
+            }
+            if (accept) {
+                found = true;
+                next = r.skip;
+                break;
+            }
+            k = k + 1;
         }
-        if (accept) {
+        if (!__any_sync(0xffffffffu, found)) break;
+        if (found) {
             const NodeRec64 q = rec64[k];
             if (q.mass != 0) {
                 const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py), dz = A::sub(q.cz, pz);
                 A::monopole_xyz(q.mass, dx, dy, dz, eps2, acx, acy, acz);
             }
-            k = r.skip;
-        } else {
-            k = k + 1;
+            k = next;
         }
     }
-    ax[me] = A::mul(acx, G);
-    ay[me] = A::mul(acy, G);
-    az[me] = A::mul(acz, G);
+    if (valid) {
+        ax[me] = A::mul(acx, G);
+        ay[me] = A::mul(acy, G);
+        az[me] = A::mul(acz, G);
+    }
 }
 
 // Per-body reference rule with FP64-accurate double-float monopoles (NB_DF64). The walk and the
