@@ -217,7 +217,17 @@ def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epoc
     acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
     tree.accel(t["x"], t["y"], t["z"], *acc, G, learned.EPS2, "theta", "f64")
     p_med, p_p99 = learned.errors(acc, ref, targets)
+    # the per-body theta rule with the learned policy's arithmetic (FP32 pairs, compensated)
+    plain32 = []
+    for th in (0.3, 0.35, 0.4, 0.5):
+        tree.set_theta(th)
+        ms = learned.timed(lambda: tree.accel(t["x"], t["y"], t["z"], *acc, G, learned.EPS2,
+                                              "theta", "f32c"))
+        med, p99 = learned.errors(acc, ref, targets)
+        plain32.append({"kind": "per-body-theta-f32c", "param": th, "ms": ms, "median": med,
+                        "p99": p99})
     tree.close()
+    bp = learned.best_within(plain32, "per-body-theta-f32c")
     bl = learned.best_within(rows, "learned")
     bt = learned.best_within(rows, "theta-walk")
     ms_plain = learned.time_steps(ctx, t, G, steps, "theta", "f64", theta=0.5)
@@ -227,6 +237,8 @@ def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epoc
     ms_t = (learned.time_steps(ctx, t, G, steps, "learned", "f32c",
                                policy=(None, 0.0, bt["param"], learned.NO_CAP))
             if bt else None)
+    ms_p32 = (learned.time_steps(ctx, t, G, steps, "theta", "f32c", theta=bp["param"])
+              if bp else None)
     out = {
         "workload": f"{n}-body 50/50 heliocentric disc + Plummer sphere (1e-3 Msun, a = 0.05 AU, "
                     f"5 AU from the central body), evaluation seed {eval_seed}; FP32 forces, FP64 "
@@ -241,10 +253,14 @@ def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epoc
                                 "within_bounds": p_med <= 1e-4 and p_p99 <= 1e-3},
         "learned_best": bl, "theta_walk_best": bt,
         "learned_ms_per_step": ms_l, "theta_walk_ms_per_step": ms_t,
+        "per_body_theta_f32c": plain32, "per_body_theta_f32c_best": bp,
+        "per_body_theta_f32c_ms_per_step": ms_p32,
     }
     if ms_l:
         out["learned_steps_per_s"] = 1e3 / ms_l
         out["speedup_vs_plain_theta0.5_fp64"] = ms_plain / ms_l
         if ms_t:
             out["speedup_vs_theta_walk_matched_error"] = ms_t / ms_l
+        if ms_p32:
+            out["speedup_vs_per_body_theta_f32c_matched_error"] = ms_p32 / ms_l
     return out
