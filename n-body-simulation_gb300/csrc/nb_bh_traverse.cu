@@ -143,72 +143,83 @@ bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __res
                      const double* __restrict__ x, const double* __restrict__ y,
                      const double* __restrict__ z, const double* __restrict__ box, uint32_t n,
                      double theta, double eps2, double G, double* __restrict__ ax,
-                     double* __restrict__ ay, double* __restrict__ az) {
+                     double* __restrict__ ay, double* __restrict__ az,
+                     uint32_t* __restrict__ next_group) {
     using A = Arith<MODE>;
-    const uint32_t p = blockIdx.x * TR_THREADS + threadIdx.x;
-    const bool valid = p < n;  // lanes past the end stay (they take part in the warp votes)
-    const uint32_t nn = info[0];
-    const uint32_t me = valid ? ids[p] : NB_NONE;
-    const double px = valid ? x[me] : 0.0, py = valid ? y[me] : 0.0, pz = valid ? z[me] : 0.0;
-    const double E = box[6];
-    const double ox = box[0] + E / 2, oy = box[1] + E / 2, oz = box[2] + E / 2;
-    const float pxf = (float)(px - ox), pyf = (float)(py - oy), pzf = (float)(pz - oz);
-    const float th2 = (float)(theta * theta);
-    const float u4 = 4.0f * 5.9604645e-8f;  // 4 * 2^-24
-    const float Ef = (float)E;
-    double acx = 0, acy = 0, acz = 0;
-    uint32_t k = valid ? 0u : nn;
-    // Find, then compute: every lane walks (FP32 tests, divergent but off the FP64 pipe) to its
-    // next accepted cell, then the lanes evaluate their FP64 monopoles together, so the FP64
-    // work runs with all unfinished lanes instead of the few that accept in the same iteration.
+    const uint32_t n_groups = (n + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    // persistent warps: each takes the next 32 bodies until none are left, so no warp waits for
+    // its block's slowest warp and the last wave's tail is one group long
     for (;;) {
-        bool found = false;
-        uint32_t next = 0;
-        while (k < nn) {
-            const NodeRec32 r = rec32[k];
-            if (r.body == me) {
-                k = r.skip;
-                continue;
-            }
-            bool accept = r.body != NB_NONE;
-            if (!accept) {
-                const float dxf = r.cx - pxf, dyf = r.cy - pyf, dzf = r.cz - pzf;
-                const float d2f = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
-                const float t = th2 * d2f;
-                const float rel = u4 * (3.5f * Ef * nb_rsqrt_f32(d2f) + 8.0f);
-                const float margin = t * rel + u4 * r.edge2;
-                if (r.edge2 > t + margin) {
-                    accept = false;  // certainly opened
-                } else if (r.edge2 < t - margin) {
-                    accept = true;   // certainly accepted
-                } else {             // undecided: the reference's FP64 expression
-                    const NodeRec64 q = rec64[k];
-                    const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py),
-                                 dz = A::sub(q.cz, pz);
-                    accept = A::mul(q.edge, A::rsqrt(A::norm2(dx, dy, dz))) < theta;
+        uint32_t grp = 0;
+        if (lane == 0) grp = atomicAdd(next_group, 1u);
+        grp = __shfl_sync(0xffffffffu, grp, 0);
+        if (grp >= n_groups) break;
+        const uint32_t p = grp * 32 + lane;
+        const bool valid = p < n;  // lanes past the end stay (they take part in the warp votes)
+        const uint32_t nn = info[0];
+        const uint32_t me = valid ? ids[p] : NB_NONE;
+        const double px = valid ? x[me] : 0.0, py = valid ? y[me] : 0.0, pz = valid ? z[me] : 0.0;
+        const double E = box[6];
+        const double ox = box[0] + E / 2, oy = box[1] + E / 2, oz = box[2] + E / 2;
+        const float pxf = (float)(px - ox), pyf = (float)(py - oy), pzf = (float)(pz - oz);
+        const float th2 = (float)(theta * theta);
+        const float u4 = 4.0f * 5.9604645e-8f;  // 4 * 2^-24
+        const float Ef = (float)E;
+        double acx = 0, acy = 0, acz = 0;
+        uint32_t k = valid ? 0u : nn;
+        // Find, then compute: every lane walks (FP32 tests, divergent but off the FP64 pipe) to its
+        // next accepted cell, then the lanes evaluate their FP64 monopoles together, so the FP64
+        // work runs with all unfinished lanes instead of the few that accept in the same iteration.
+        for (;;) {
+            bool found = false;
+            uint32_t next = 0;
+            while (k < nn) {
+                const NodeRec32 r = rec32[k];
+                if (r.body == me) {
+                    k = r.skip;
+                    continue;
                 }
+                bool accept = r.body != NB_NONE;
+                if (!accept) {
+                    const float dxf = r.cx - pxf, dyf = r.cy - pyf, dzf = r.cz - pzf;
+                    const float d2f = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
+                    const float t = th2 * d2f;
+                    const float rel = u4 * (3.5f * Ef * nb_rsqrt_f32(d2f) + 8.0f);
+                    const float margin = t * rel + u4 * r.edge2;
+                    if (r.edge2 > t + margin) {
+                        accept = false;  // certainly opened
+                    } else if (r.edge2 < t - margin) {
+                        accept = true;   // certainly accepted
+                    } else {             // undecided: the reference's FP64 expression
+                        const NodeRec64 q = rec64[k];
+                        const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py),
+                                     dz = A::sub(q.cz, pz);
+                        accept = A::mul(q.edge, A::rsqrt(A::norm2(dx, dy, dz))) < theta;
+                    }
+                }
+                if (accept) {
+                    found = true;
+                    next = r.skip;
+                    break;
+                }
+                k = k + 1;
             }
-            if (accept) {
-                found = true;
-                next = r.skip;
-                break;
+            if (!__any_sync(0xffffffffu, found)) break;
+            if (found) {
+                const NodeRec64 q = rec64[k];
+                if (q.mass != 0) {
+                    const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py), dz = A::sub(q.cz, pz);
+                    A::monopole_xyz(q.mass, dx, dy, dz, eps2, acx, acy, acz);
+                }
+                k = next;
             }
-            k = k + 1;
         }
-        if (!__any_sync(0xffffffffu, found)) break;
-        if (found) {
-            const NodeRec64 q = rec64[k];
-            if (q.mass != 0) {
-                const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py), dz = A::sub(q.cz, pz);
-                A::monopole_xyz(q.mass, dx, dy, dz, eps2, acx, acy, acz);
-            }
-            k = next;
+        if (valid) {
+            ax[me] = A::mul(acx, G);
+            ay[me] = A::mul(acy, G);
+            az[me] = A::mul(acz, G);
         }
-    }
-    if (valid) {
-        ax[me] = A::mul(acx, G);
-        ay[me] = A::mul(acy, G);
-        az[me] = A::mul(acz, G);
     }
 }
 
@@ -551,6 +562,27 @@ bh_count_kernel(const NodeRec64* __restrict__ rec, const uint32_t* __restrict__ 
 // walk (bh_theta_f64_kernel). Both produce identical results; the switch exists for comparison.
 int g_lockstep = 0;
 
+// Persistent launch of bh_theta_lane_kernel: resident blocks only, groups from work[1].
+template <int MODE>
+nb_status launch_lane(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const double* y,
+                      const double* z, double* ax, double* ay, double* az, double G, double eps2,
+                      cudaStream_t s) {
+    static int per_sm[2] = {0, 0};
+    int& ps = per_sm[MODE == IEEE64 ? 0 : 1];
+    if (ps == 0) {
+        NB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, bh_theta_lane_kernel<MODE>,
+                                                                  TR_THREADS, 0));
+        if (ps < 1) ps = 1;
+    }
+    int grid = nb::ceil_div(t->n, TR_THREADS);
+    if (grid > ctx->sm_count * ps) grid = ctx->sm_count * ps;
+    NB_CUDA_TRY(cudaMemsetAsync(t->work + 1, 0, sizeof(uint32_t), s));
+    bh_theta_lane_kernel<MODE><<<grid, TR_THREADS, 0, s>>>(
+        t->rec32, t->rec64, t->info, t->ids, x, y, z, t->box, t->n, t->params.theta, eps2, G, ax,
+        ay, az, t->work + 1);
+    return nb::check_launch(MODE == IEEE64 ? "bh_theta_lane_kernel<ieee>" : "bh_theta_lane_kernel");
+}
+
 }  // namespace
 
 namespace nb {
@@ -586,20 +618,14 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
                         t->rec64, t->info, t->ids, x, y, z, n, theta, eps2, G, ax, ay, az);
                     return nb::check_launch("bh_theta_f64_kernel<ieee>");
                 }
-                bh_theta_lane_kernel<IEEE64><<<grid, TR_THREADS, 0, s>>>(
-                    t->rec32, t->rec64, t->info, t->ids, x, y, z, t->box, n, theta, eps2, G, ax,
-                    ay, az);
-                return nb::check_launch("bh_theta_lane_kernel<ieee>");
+                return launch_lane<IEEE64>(ctx, t, x, y, z, ax, ay, az, G, eps2, s);
             case NB_F64:
                 if (g_lockstep) {
                     bh_theta_f64_kernel<FAST64><<<grid, TR_THREADS, 0, s>>>(
                         t->rec64, t->info, t->ids, x, y, z, n, theta, eps2, G, ax, ay, az);
                     return nb::check_launch("bh_theta_f64_kernel");
                 }
-                bh_theta_lane_kernel<FAST64><<<grid, TR_THREADS, 0, s>>>(
-                    t->rec32, t->rec64, t->info, t->ids, x, y, z, t->box, n, theta, eps2, G, ax,
-                    ay, az);
-                return nb::check_launch("bh_theta_lane_kernel");
+                return launch_lane<FAST64>(ctx, t, x, y, z, ax, ay, az, G, eps2, s);
             case NB_DF64:
                 if (t->G == 0)
                     return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: NB_DF64 needs a build with G != 0");
