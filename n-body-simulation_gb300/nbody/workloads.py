@@ -3,8 +3,9 @@
 * ``precision_form``: naive all-pairs with FP32 pair math and compensated accumulation against
   the FP64 GPU oracle on a 262,144-body Plummer sphere (G = M = a = 1, softening 1e-3): force
   error of sampled bodies, pair throughput against the FP32 FMA and SFU (rsqrt) peaks, energy
-  drift over a leapfrog run with dt = 1e-3, and the FP32/FP64 trajectory difference after a few
-  steps.
+  drift over a leapfrog run with dt = 1e-3, the FP32/FP64 trajectory difference after a few
+  steps, and the FP32C and FP64 energy drifts over the same 1,000 steps on a 16,384-body sphere
+  (where the FP64 run is affordable).
 * ``batched_ensemble``: 512 independent Plummer spheres with N log-uniform in [256, 16384], FP32
   forces and FP64 leapfrog, all systems in one persistent pair-kernel launch per step replayed
   from a captured CUDA graph, tile configuration from the autotuner; against one launch per
@@ -66,7 +67,7 @@ def _leapfrog(ctx, t, acc, vh, G, eps2, dt, steps, precision):
 
 def precision_form(ctx: Context, n: int = 262144, steps: int = 1000, dt: float = 1e-3,
                    softening: float = 1e-3, fp64_steps: int = 5, n_targets: int = 4096,
-                   seed: int = 1):
+                   seed: int = 1, drift_n: int = 16384):
     import torch
     d = generators.plummer(n, seed)
     G, eps2 = 1.0, softening * softening
@@ -106,6 +107,18 @@ def precision_form(ctx: Context, n: int = 262144, steps: int = 1000, dt: float =
     ctx.sync()
     run_s = time.perf_counter() - t0
     e1 = _energy(ctx, t, G)
+    # the same 1,000-step drift comparison on a smaller sphere, where the FP64 run is affordable
+    drift_small = {}
+    ds = generators.plummer(drift_n, seed)
+    for prec in ("f32c", "f64"):
+        ts = learned.device_system(ds)
+        a = [torch.zeros(drift_n, dtype=torch.float64, device="cuda") for _ in range(3)]
+        vh2 = [torch.zeros_like(v) for v in a]
+        f0 = _energy(ctx, ts, G)
+        ctx.naive_accel(ts["m"], ts["x"], ts["y"], ts["z"], *a, G, eps2, prec)
+        _leapfrog(ctx, ts, a, vh2, G, eps2, dt, steps, prec)
+        f1 = _energy(ctx, ts, G)
+        drift_small[prec] = abs(f1[2] - f0[2]) / abs(f0[2])
     return {
         "workload": f"naive all-pairs, {n}-body Plummer sphere (G=M=a=1, seed {seed}), "
                     f"softening {softening}",
@@ -118,6 +131,7 @@ def precision_form(ctx: Context, n: int = 262144, steps: int = 1000, dt: float =
         "energy_drift_f32c": {"steps": steps, "dt": dt, "E0": e0[2], "E1": e1[2],
                               "rel": abs(e1[2] - e0[2]) / abs(e0[2]), "run_s": run_s},
         "f32c_vs_f64_max_position_diff": {"steps": fp64_steps, "value": dpos},
+        "energy_drift_f32c_vs_f64": {"bodies": drift_n, "steps": steps, "dt": dt, **drift_small},
     }
 
 
