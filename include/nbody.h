@@ -347,7 +347,8 @@ nb_status nb_bh_set_policy(nb_bh_tree* tree, const float* params_dev, float log1
                            double theta_fallback, uint32_t count_cap, uint32_t flags);
 /* NB_OPEN_LEARNED traversal that also counts, into 4 DEVICE uint64: body-cell interactions
  * (counters_dev[0]), cells decided by the policy (network, or theta rule when the policy has no
- * network) ([1]), cells visited ([2]) and walk steps of up to 32 cells ([3]), summed over groups. */
+ * network) ([1]), cells visited ([2]) and walk steps of up to 32 cells ([3]), summed over
+ * groups. */
 nb_status nb_bh_accel_learned_counted(nb_ctx* ctx, const nb_bh_tree* tree, const double* x,
                                       const double* y, const double* z, double* ax, double* ay,
                                       double* az, double eps2, unsigned long long* counters_dev,

@@ -235,7 +235,8 @@ bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __res
 // Neumaier-compensated (hi + running lo), converted to FP64 at the end and scaled by G / G_build.
 __global__ void __launch_bounds__(TR_THREADS)
 bh_theta_df_kernel(const NodeRec32* __restrict__ rec32, const float4* __restrict__ rec32lo,
-                   const float4* __restrict__ rec32lo2, const NodeRec64* __restrict__ rec64, const uint32_t* __restrict__ info,
+                   const float4* __restrict__ rec32lo2, const NodeRec64* __restrict__ rec64,
+                   const uint32_t* __restrict__ info,
                    const uint32_t* __restrict__ ids, const double* __restrict__ x,
                    const double* __restrict__ y, const double* __restrict__ z,
                    const double* __restrict__ box, uint32_t n, double theta, double eps2,
@@ -628,10 +629,11 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
                 return launch_lane<FAST64>(ctx, t, x, y, z, ax, ay, az, G, eps2, s);
             case NB_DF64:
                 if (t->G == 0)
-                    return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: NB_DF64 needs a build with G != 0");
+                    return nb::set_error(NB_ERR_INVALID_ARG,
+                                         "nb_bh_accel: NB_DF64 needs a build with G != 0");
                 bh_theta_df_kernel<<<grid, TR_THREADS, 0, s>>>(
-                    t->rec32, t->rec32lo, t->rec32lo2, t->rec64, t->info, t->ids, x, y, z, t->box, n, theta,
-                    eps2, G / t->G, ax, ay, az);
+                    t->rec32, t->rec32lo, t->rec32lo2, t->rec64, t->info, t->ids, x, y, z, t->box,
+                    n, theta, eps2, G / t->G, ax, ay, az);
                 return nb::check_launch("bh_theta_df_kernel");
             case NB_F32C:
                 if (G != t->G)

@@ -180,7 +180,8 @@ __device__ __forceinline__ nb_df df_sqr(nb_df a) {
 // with h = fl(x), m = fl(x - h), l = fl(x - h - m): 72 bits, so FP64 values are exact). The two
 // leading differences are error-free, so the result is accurate to ~2^-48 of the difference
 // itself however close the two numbers are.
-__device__ __forceinline__ nb_df tf_diff(float ch, float cm, float cl, float ph, float pm, float pl) {
+__device__ __forceinline__ nb_df tf_diff(float ch, float cm, float cl, float ph, float pm,
+                                         float pl) {
     const nb_df s = df_two_sum(ch, -ph);
     const nb_df t = df_two_sum(cm, -pm);
     const nb_df u = df_two_sum(s.h, t.h);

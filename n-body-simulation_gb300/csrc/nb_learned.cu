@@ -65,10 +65,10 @@ __device__ GroupGeo group_geo(bool valid, float px, float py, float pz, float a_
 
 // The 8 features of a (group, cell) pair and the cell's class: 0 = decide with the network,
 // 1 = body leaf (accept), 2 = may overlap the group (open), 3 = outside the training range
-// (theta rule), 4 = provably accurate enough (accept). gap = the smallest distance from a member of the group to the cell's centre of
-// mass; d = distance from the group's box centre. Ratios use the fast reciprocal and logarithms
-// the fast base-2 logarithm (features only steer the policy; labels and training use the same
-// function).
+// (theta rule), 4 = provably accurate enough (accept). gap = the smallest distance from a member
+// of the group to the cell's centre of mass; d = distance from the group's box centre. Ratios use
+// the fast reciprocal and logarithms the fast base-2 logarithm (features only steer the policy;
+// labels and training use the same function).
 //
 // Class 4 (accept without the network; only when bound_tau > 0): the cell's bodies lie within
 // b = sqrt(3) * edge of its centre of mass, so for a body at distance R >= gap the monopole's
@@ -318,7 +318,7 @@ constexpr int LT_CAP = 1024;        // stack entries per warp
 constexpr int LT_RESERVE = 7 * NB_MAX_TREE_DEPTH + 8;  // headroom of single-cell steps
 constexpr int LT_BATCH = 32;        // cells popped per step (one per lane)
 constexpr uint32_t LT_DIRECT = 8;   // opened cells up to this many bodies: direct sums
-constexpr int LT_LIST = 384;        // interaction list entries per warp (>= LT_BATCH * (LT_DIRECT + 1))
+constexpr int LT_LIST = 384;        // interaction list entries per warp (a full step fits)
 static_assert(LT_LIST >= LT_BATCH * (LT_DIRECT + 1), "one step must fit in an empty list");
 
 // Sum of the interactions in list[0..count) for one body; 4 independent accumulators. An entry
@@ -401,7 +401,7 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
         const uint32_t p = gw * 32 + lane;
         const bool valid = p < n;
         const uint32_t me = valid ? ids[p] : NB_NONE;
-        // own position: box-centre relative (features) and relative to the group's first body (forces)
+        // own position: box-centre relative (features), group-relative (forces)
         float4 ph = make_float4(0.f, 0.f, 0.f, 0.f), pl = ph;
         float a_prev = 0.f;
         if (valid) {
@@ -438,7 +438,7 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
         auto pop_and_load = [&]() -> int {
             __syncwarp();
             int nb = top > 0 ? min(min(LT_BATCH, top), max(1, (LT_CAP - LT_RESERVE - top) / 7)) : 0;
-            if (nb > 0 && top + 7 * nb > LT_CAP) {  // unreachable by the bound above; report and stop
+            if (nb > 0 && top + 7 * nb > LT_CAP) {  // unreachable by the bound above; report, stop
                 if (lane == 0) atomicOr(err_word, NB_DEVERR_STACK);
                 nb = 0;
             }
