@@ -495,6 +495,11 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
     out["naive_f64_disc_16384"] = {"ms_per_eval": ms, "gpairs_per_s": gp,
                                    "frac_of_measured_fp64_fma_peak":
                                        gp * 20e9 / fma_peak(ctx, fp64=True)}
+    ms = timed(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, dd["G"], EPS2, "df64"),
+               5)
+    out["naive_df64_disc_16384"] = {
+        "ms_per_eval": ms, "gpairs_per_s": n * n / (ms * 1e-3) / 1e9,
+        "arithmetic": "double-float (FP32 pairs) on the FP32 pipe, FP64-accurate to ~1e-14"}
     for name, fn in (("precision_form_naive_f32c_plummer_262144", workloads.precision_form),
                      ("batched_ensemble_512_plummer", workloads.batched_ensemble),
                      ("learned_opening_bh_mix_1M", workloads.learned_form)):

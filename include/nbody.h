@@ -51,7 +51,8 @@ typedef enum nb_precision {
                          of the reference's formula */
     NB_F32C = 2,      /* FP32 pair math, compensated (TwoSum) per-body accumulation */
     NB_DF64 = 3       /* FP64-accurate double-float (pairs of FP32, ~2^-48 per operation) on the
-                         FP32 pipe: Barnes-Hut per-body rule only, same accepted cells as NB_F64 */
+                         FP32 pipe: naive all-pairs, and the Barnes-Hut per-body rule (same
+                         accepted cells as NB_F64) */
 } nb_precision;
 
 #define NB_MAX_TREE_DEPTH 42

@@ -10,6 +10,7 @@
 //  * NB_F32C: the FP32-compensated pair kernel of nb_pair.cuh (scalar FP32 pair math, TwoSum
 //    accumulation, stream-K persistent CTAs, cp.async.bulk j-tiles behind bounded mbarrier
 //    waits), run as a batch of one system.
+//  * NB_DF64: double-float pair math on the FP32 pipe (FP64-accurate to ~1e-14).
 #include "nb_internal.cuh"
 #include "nb_pair.cuh"
 
@@ -20,12 +21,16 @@ namespace {
 // ---------------------------------------------------------------------------------------------
 constexpr int F64_THREADS = 64;
 
+// blockIdx.y selects a chunk of `chunk` sources (NB_F64 at small n, for more warps per SM; the
+// IEEE mode always runs one chunk so that its sum order stays the reference's); with more than
+// one chunk the partial sums (times G) go to part[(chunk index * n_t + target) * 3 + axis].
 template <bool IEEE>
 __global__ void __launch_bounds__(F64_THREADS)
 naive_f64_kernel(const double* __restrict__ m, const double* __restrict__ x,
                  const double* __restrict__ y, const double* __restrict__ z,
                  double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az,
-                 uint32_t n, uint32_t i_begin, uint32_t i_end, double G, double eps2) {
+                 uint32_t n, uint32_t i_begin, uint32_t i_end, double G, double eps2,
+                 uint32_t chunk, double* __restrict__ part) {
     __shared__ double sx[F64_THREADS], sy[F64_THREADS], sz[F64_THREADS], sm[F64_THREADS];
     const uint32_t i = i_begin + blockIdx.x * F64_THREADS + threadIdx.x;
     const bool active = i < i_end;
@@ -36,16 +41,17 @@ naive_f64_kernel(const double* __restrict__ m, const double* __restrict__ x,
         pz = z[i];
     }
     double acc_x = 0, acc_y = 0, acc_z = 0;
-    for (uint32_t k = 0; k < n; k += F64_THREADS) {
+    const uint32_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+    for (uint32_t k = j0; k < j1; k += F64_THREADS) {
         const uint32_t j = k + threadIdx.x;
-        if (j < n) {
+        if (j < j1) {
             sx[threadIdx.x] = x[j];
             sy[threadIdx.x] = y[j];
             sz[threadIdx.x] = z[j];
             sm[threadIdx.x] = m[j];
         }
         __syncthreads();
-        const uint32_t cnt = min((uint32_t)F64_THREADS, n - k);
+        const uint32_t cnt = min((uint32_t)F64_THREADS, j1 - k);
         if (active) {
             if (IEEE) {
                 for (uint32_t jj = 0; jj < cnt; ++jj) {
@@ -82,12 +88,48 @@ naive_f64_kernel(const double* __restrict__ m, const double* __restrict__ x,
             ax[i] = __dmul_rn(acc_x, G);
             ay[i] = __dmul_rn(acc_y, G);
             az[i] = __dmul_rn(acc_z, G);
-        } else {
+        } else if (gridDim.y == 1) {
             ax[i] = acc_x * G;
             ay[i] = acc_y * G;
             az[i] = acc_z * G;
+        } else {
+            double* o = part + ((size_t)blockIdx.y * (i_end - i_begin) + (i - i_begin)) * 3;
+            o[0] = acc_x * G;
+            o[1] = acc_y * G;
+            o[2] = acc_z * G;
         }
     }
+}
+
+// Adds the chunks' partial sums of each target in chunk order.
+__global__ void chunk_combine_kernel(const double* __restrict__ part, uint32_t chunks,
+                                  uint32_t i_begin, uint32_t i_end, double* __restrict__ ax,
+                                  double* __restrict__ ay, double* __restrict__ az) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n_t = i_end - i_begin;
+    if (t >= n_t) return;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (uint32_t c = 0; c < chunks; ++c) {
+        const double* o = part + ((size_t)c * n_t + t) * 3;
+        sx += o[0];
+        sy += o[1];
+        sz += o[2];
+    }
+    ax[i_begin + t] = sx;
+    ay[i_begin + t] = sy;
+    az[i_begin + t] = sz;
+}
+
+// Number and size (a multiple of `tile`) of the source chunks that give at least ~8 warps per SM
+// when blocks_per_chunk blocks cover the targets.
+void choose_chunks(const nb_ctx* ctx, int blocks_per_chunk, uint32_t n, uint32_t tile,
+                   uint32_t* chunks, uint32_t* chunk) {
+    uint32_t c = (uint32_t)nb::ceil_div(8LL * ctx->sm_count, blocks_per_chunk);
+    c = min(c, 32u);
+    c = min(c, (uint32_t)nb::ceil_div(n, tile));
+    if (c < 1) c = 1;
+    *chunk = (uint32_t)nb::ceil_div(nb::ceil_div(n, c), tile) * tile;
+    *chunks = (uint32_t)nb::ceil_div(n, *chunk);
 }
 
 // FP64 accelerations of listed target bodies (ax[t] for targets[t]); FMAs + refined rsqrt.
@@ -186,6 +228,140 @@ nb_status naive_f32c(nb_ctx* ctx, const double* m, const double* x, const double
                            ctx->dev_error, stream);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Double-float (NB_DF64): FP64-accurate pair math on the FP32 pipe
+// ---------------------------------------------------------------------------------------------
+constexpr int DF_THREADS = 128;
+constexpr int DF_TILE = 128;
+
+// Source record: the position minus body 0 (exact) as triple-floats and G*m as a double-float.
+struct __align__(16) SrcTF {
+    float xh, xm, xl, yh, ym, yl, zh, zm, zl, gh, gl, pad;
+};
+
+__global__ void df_prepare_kernel(const double* __restrict__ m, const double* __restrict__ x,
+                                  const double* __restrict__ y, const double* __restrict__ z,
+                                  uint32_t n, double G, SrcTF* __restrict__ out) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    SrcTF r;
+    tf_split_diff(x[b], x[0], r.xh, r.xm, r.xl);
+    tf_split_diff(y[b], y[0], r.yh, r.ym, r.yl);
+    tf_split_diff(z[b], z[0], r.zh, r.zm, r.zl);
+    const double gm = G * m[b];
+    r.gh = (float)gm;
+    r.gl = (float)(gm - (double)r.gh);
+    r.pad = 0.f;
+    out[b] = r;
+}
+
+// One thread per target; sources in shared-memory tiles. Per pair: exact separations from the
+// triple-floats, r^2 + eps^2 with TwoSums, 1/r from the hardware estimate with an error-free
+// correction, G m / r^3 and the products in double-float (the same arithmetic as the
+// Barnes-Hut double-float monopole), Neumaier-compensated sums per tile added into FP64. The
+// self pair contributes exactly 0.
+// blockIdx.y selects a chunk of `chunk` sources; with more than one chunk the partial sums go
+// to part[(chunk index * n_t + target) * 3 + axis] and df_combine_kernel adds them in order.
+__global__ void __launch_bounds__(DF_THREADS)
+naive_df_kernel(const SrcTF* __restrict__ src, uint32_t n, uint32_t i_begin, uint32_t i_end,
+                uint32_t chunk, float e2h, float e2l, double* __restrict__ ax,
+                double* __restrict__ ay, double* __restrict__ az, double* __restrict__ part) {
+    __shared__ SrcTF tile[DF_TILE];
+    const uint32_t i = i_begin + blockIdx.x * DF_THREADS + threadIdx.x;
+    const bool active = i < i_end;
+    SrcTF me{};
+    if (active) me = src[i];
+    double sum_x = 0.0, sum_y = 0.0, sum_z = 0.0;
+    const uint32_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+    for (uint32_t k = j0; k < j1; k += DF_TILE) {
+        float ahx = 0.f, ahy = 0.f, ahz = 0.f, alx = 0.f, aly = 0.f, alz = 0.f;
+        for (uint32_t j = threadIdx.x; j < DF_TILE && k + j < j1; j += DF_THREADS)
+            tile[j] = src[k + j];
+        __syncthreads();
+        const uint32_t cnt = min((uint32_t)DF_TILE, j1 - k);
+        if (active) {
+            for (uint32_t jj = 0; jj < cnt; ++jj) {
+                const SrcTF c = tile[jj];
+                const nb_df dx = tf_diff(c.xh, c.xm, c.xl, me.xh, me.xm, me.xl);
+                const nb_df dy = tf_diff(c.yh, c.ym, c.yl, me.yh, me.ym, me.yl);
+                const nb_df dz = tf_diff(c.zh, c.zm, c.zl, me.zh, me.zm, me.zl);
+                const nb_df sx = df_sqr(dx), sy = df_sqr(dy), sz = df_sqr(dz);
+                nb_df a = df_two_sum(sx.h, sy.h);
+                a.l += sx.l + sy.l;
+                nb_df b = df_two_sum(a.h, sz.h);
+                b.l += a.l + sz.l;
+                nb_df e = df_two_sum(b.h, e2h);
+                e.l += b.l + e2l;
+                const nb_df r2 = df_two_sum(e.h, e.l);
+                const float y0 = nb_rsqrt_f32(r2.h);
+                const float q = y0 * y0, qe = fmaf(y0, y0, -q);
+                const float th = r2.h * q;
+                float te = fmaf(r2.h, q, -th);
+                te = fmaf(r2.h, qe, te);
+                te = fmaf(r2.l, q, te);
+                const float ee = (1.0f - th) - te;
+                const nb_df inv = df_fast_two_sum(y0, y0 * (ee * fmaf(0.375f, ee, 0.5f)));
+                const nb_df w = df_mul(nb_df{c.gh, c.gl}, df_mul(df_sqr(inv), inv));
+                const nb_df tx = df_mul(dx, w), ty = df_mul(dy, w), tz = df_mul(dz, w);
+                nb_df t = df_two_sum(ahx, tx.h);
+                ahx = t.h;
+                alx += t.l + tx.l;
+                t = df_two_sum(ahy, ty.h);
+                ahy = t.h;
+                aly += t.l + ty.l;
+                t = df_two_sum(ahz, tz.h);
+                ahz = t.h;
+                alz += t.l + tz.l;
+            }
+            // the tile's compensated sum into FP64 (3 FP64 adds per tile): the FP32 low part
+            // of a compensated sum over all n terms would lose digits at large n
+            sum_x += (double)ahx + (double)alx;
+            sum_y += (double)ahy + (double)aly;
+            sum_z += (double)ahz + (double)alz;
+        }
+        __syncthreads();
+    }
+    if (!active) return;
+    if (gridDim.y == 1) {
+        ax[i] = sum_x;
+        ay[i] = sum_y;
+        az[i] = sum_z;
+    } else {
+        double* o = part + ((size_t)blockIdx.y * (i_end - i_begin) + (i - i_begin)) * 3;
+        o[0] = sum_x;
+        o[1] = sum_y;
+        o[2] = sum_z;
+    }
+}
+
+
+nb_status naive_df64(nb_ctx* ctx, const double* m, const double* x, const double* y,
+                     const double* z, double* ax, double* ay, double* az, uint32_t n,
+                     uint32_t i_begin, uint32_t i_end, double G, double eps2,
+                     cudaStream_t stream) {
+    // split the sources into chunks when the targets alone give too few warps per SM
+    const uint32_t n_t = i_end - i_begin;
+    const int blocks = nb::ceil_div(n_t, DF_THREADS);
+    uint32_t chunks = 1, chunk = n;
+    choose_chunks(ctx, blocks, n, DF_TILE, &chunks, &chunk);
+    const size_t src_bytes = ((size_t)n * sizeof(SrcTF) + 255) & ~(size_t)255;
+    const size_t part_bytes = chunks > 1 ? (size_t)chunks * n_t * 3 * sizeof(double) : 0;
+    void* base = nullptr;
+    NB_TRY(nb::scratch(ctx, NB_SCRATCH_NAIVE_DF, src_bytes + part_bytes, &base));
+    SrcTF* src = (SrcTF*)base;
+    double* part = (double*)((char*)base + src_bytes);
+    df_prepare_kernel<<<nb::ceil_div(n, 256), 256, 0, stream>>>(m, x, y, z, n, G, src);
+    NB_TRY(nb::check_launch("df_prepare_kernel"));
+    const float e2h = (float)eps2, e2l = (float)(eps2 - (double)e2h);
+    naive_df_kernel<<<dim3(blocks, chunks), DF_THREADS, 0, stream>>>(
+        src, n, i_begin, i_end, chunk, e2h, e2l, ax, ay, az, part);
+    NB_TRY(nb::check_launch("naive_df_kernel"));
+    if (chunks == 1) return NB_OK;
+    chunk_combine_kernel<<<nb::ceil_div(n_t, 256), 256, 0, stream>>>(part, chunks, i_begin,
+                                                                     i_end, ax, ay, az);
+    return nb::check_launch("chunk_combine_kernel");
+}
+
 nb_status naive_dispatch(nb_ctx* ctx, const double* m, const double* x, const double* y,
                          const double* z, double* ax, double* ay, double* az, uint32_t n,
                          uint32_t i_begin, uint32_t i_end, double G, double eps2,
@@ -199,16 +375,30 @@ nb_status naive_dispatch(nb_ctx* ctx, const double* m, const double* x, const do
     switch (prec) {
         case NB_F64_IEEE:
             naive_f64_kernel<true><<<nb::ceil_div(n_t, F64_THREADS), F64_THREADS, 0, stream>>>(
-                m, x, y, z, ax, ay, az, n, i_begin, i_end, G, eps2);
+                m, x, y, z, ax, ay, az, n, i_begin, i_end, G, eps2, n, nullptr);
             return nb::check_launch("naive_f64_kernel<ieee>");
-        case NB_F64:
-            naive_f64_kernel<false><<<nb::ceil_div(n_t, F64_THREADS), F64_THREADS, 0, stream>>>(
-                m, x, y, z, ax, ay, az, n, i_begin, i_end, G, eps2);
-            return nb::check_launch("naive_f64_kernel");
+        case NB_F64: {
+            const int blocks = nb::ceil_div(n_t, F64_THREADS);
+            uint32_t chunks = 1, chunk = n;
+            choose_chunks(ctx, blocks, n, F64_THREADS, &chunks, &chunk);
+            double* part = nullptr;
+            if (chunks > 1) {
+                void* base = nullptr;
+                NB_TRY(nb::scratch(ctx, NB_SCRATCH_NAIVE_DF, (size_t)chunks * n_t * 3 * 8, &base));
+                part = (double*)base;
+            }
+            naive_f64_kernel<false><<<dim3(blocks, chunks), F64_THREADS, 0, stream>>>(
+                m, x, y, z, ax, ay, az, n, i_begin, i_end, G, eps2, chunk, part);
+            NB_TRY(nb::check_launch("naive_f64_kernel"));
+            if (chunks == 1) return NB_OK;
+            chunk_combine_kernel<<<nb::ceil_div(n_t, 256), 256, 0, stream>>>(part, chunks, i_begin,
+                                                                             i_end, ax, ay, az);
+            return nb::check_launch("chunk_combine_kernel");
+        }
         case NB_F32C:
             return naive_f32c(ctx, m, x, y, z, ax, ay, az, n, i_begin, i_end, G, eps2, stream);
         case NB_DF64:
-            return nb::set_error(NB_ERR_UNSUPPORTED, "nb_naive_accel: NB_DF64 is a Barnes-Hut mode");
+            return naive_df64(ctx, m, x, y, z, ax, ay, az, n, i_begin, i_end, G, eps2, stream);
         default:
             return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_accel: unknown precision %d",
                                  (int)prec);

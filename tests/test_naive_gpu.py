@@ -1,8 +1,9 @@
 """Parity of the naive path (nb_naive_accel) against the CPU oracle restating
 NaiveAlgorithm.cpp:262-360, through the C ABI.
 
-Tolerances: NB_F64_IEEE bit-identical; NB_F64 per-body relative error <= 1e-12; NB_F32C per-body
-relative error median <= 1e-5 and max <= 1e-3 (Plummer, eps = 1e-3) / median <= 1e-4 (disc).
+Tolerances: NB_F64_IEEE bit-identical; NB_F64 per-body relative error <= 1e-12; NB_DF64 median
+relative error <= 1e-12; NB_F32C per-body relative error median <= 1e-5 and max <= 1e-3
+(Plummer, eps = 1e-3) / median <= 1e-4 (disc).
 """
 
 import numpy as np
@@ -51,6 +52,24 @@ def test_f64_fast_within_1e12(ctx, kind, n, eps2):
     got = run_naive(ctx, d, eps2, "f64")
     err = rel_err(*got, *ref)
     assert err.max() <= 1e-12, err.max()
+
+
+@pytest.mark.parametrize("kind,n,eps2", [("disc", 16384, 1e-22), ("plummer", 5000, 1e-6),
+                                         ("disc", 1, 1e-22), ("plummer", 129, 1e-6)])
+def test_df64_fp64_accurate(ctx, kind, n, eps2):
+    """Double-float pair math: per-body error against the FP64 oracle relative to
+    max(|a|, median |a|) <= 1e-11 and median relative error <= 1e-12 (each pair term carries
+    ~2^-46 against FP64's ~2^-52)."""
+    d = bodies(kind, n, seed=4)
+    ref = oracle.naive_accel(d["m"], d["x"], d["y"], d["z"], d["G"], eps2)
+    got = run_naive(ctx, d, eps2, "df64")
+    if n == 1:
+        assert all(np.all(g == 0) for g in got)  # the self pair alone contributes exactly 0
+        return
+    diff = np.sqrt(sum((g - r) ** 2 for g, r in zip(got, ref)))
+    mag = np.sqrt(sum(r * r for r in ref))
+    assert np.median(rel_err(*got, *ref)) <= 1e-12
+    assert (diff / np.maximum(mag, np.median(mag))).max() <= 1e-11
 
 
 @pytest.mark.parametrize("n", [1, 100, 1023, 1024, 1025, 3000, 20000])
