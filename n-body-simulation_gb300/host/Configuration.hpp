@@ -18,7 +18,7 @@ extern bool use_GPUs;
 // additions of this build (no reference counterpart): the reference fixes G in AU^3 kg^-1 d^-2
 // and FP64 pair arithmetic; these select another unit system and the precision form
 extern double G;             // 0 = the reference's G (nBodyAlgorithm.hpp:55-61)
-extern std::string precision;  // "f64" (default), "f64_ieee", "f32c", "df64" (Barnes-Hut)
+extern std::string precision;  // "f64" (default), "f64_ieee", "f32c", "df64"
 extern std::string opening;    // "theta" (default, the reference's rule) or "group"
 
 namespace naive_algorithm {

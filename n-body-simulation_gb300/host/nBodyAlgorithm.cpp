@@ -72,7 +72,7 @@ nb_precision nBodyAlgorithm::precisionMode() const {
     if (configuration::precision == "f64") return NB_F64;
     if (configuration::precision == "f64_ieee") return NB_F64_IEEE;
     if (configuration::precision == "f32c") return NB_F32C;
-    if (configuration::precision == "df64") return NB_DF64;  // Barnes-Hut only
+    if (configuration::precision == "df64") return NB_DF64;
     throw std::invalid_argument("precision must be f64, f64_ieee, f32c or df64");
 }
 
