@@ -6,6 +6,9 @@
     python n-body-simulation_gb300/nbody/cases.py learned [N] [log10_tau] [pairs]
         seeded disc + Plummer mix: labelled pairs and a short training of the opening network,
         then three learned traversals (bh_learned_kernel) at threshold tau
+    python n-body-simulation_gb300/nbody/cases.py df64 [N]
+        seeded heliocentric disc: three double-float Barnes-Hut traversals (bh_theta_df_kernel,
+        theta = 0.5) and one double-float naive evaluation (naive_df_kernel)
 
 Each case prints "ok" when its launches finished without a device error. The headline FP64
 traversal is profiled through bench.py itself (`--bodies`, `--quick`).
@@ -53,13 +56,32 @@ def learned_case(n: int = 262144, log10_tau: float = -4.25, pairs: int = 2_000_0
     ctx.sync()
 
 
+def df64_case(n: int = 262144):
+    import torch
+
+    from nbody import generators, learned
+    from nbody.lib import BHTree, Context
+    ctx = Context(0)
+    d = generators.heliocentric_disc(n, 1)
+    t = learned.device_system(d)
+    tree = BHTree(ctx, n, theta=0.5)
+    tree.build(t["m"], t["x"], t["y"], t["z"], d["G"])
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    for _ in range(3):
+        tree.accel(t["x"], t["y"], t["z"], *acc, d["G"], learned.EPS2, "theta", "df64")
+    ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, d["G"], learned.EPS2, "df64")
+    ctx.sync()
+
+
 def main(argv):
-    if not argv or argv[0] not in ("pair", "learned"):
+    if not argv or argv[0] not in ("pair", "learned", "df64"):
         print(__doc__)
         return 2
     args = argv[1:]
     if argv[0] == "pair":
         pair_case(int(args[0]) if args else 262144, int(args[1]) if len(args) > 1 else 0)
+    elif argv[0] == "df64":
+        df64_case(int(args[0]) if args else 262144)
     else:
         learned_case(int(args[0]) if args else 262144, float(args[1]) if len(args) > 1 else -4.25,
                      int(args[2]) if len(args) > 2 else 2_000_000)

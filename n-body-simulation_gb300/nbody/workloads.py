@@ -205,8 +205,8 @@ def batched_ensemble(ctx: Context, systems: int = 512, lo: int = 256, hi: int = 
 
 def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epochs: int = 4,
                  steps: int = 20, n_targets: int = 8192, eval_seed: int = 21,
-                 taus=(-4.75, -4.5, -4.25, -4.0, -3.75, -3.5),
-                 thetas=(0.3, 0.35, 0.4, 0.45, 0.5), log=None):
+                 taus=(-4.75, -4.5, -4.25, -4.125, -4.0, -3.75, -3.5),
+                 thetas=(0.3, 0.35, 0.4, 0.425, 0.45, 0.5), log=None):
     import torch
     t0 = time.perf_counter()
     X, Y = learned.training_set(ctx, n, n_pairs, log=log)
@@ -233,7 +233,7 @@ def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epoc
     p_med, p_p99 = learned.errors(acc, ref, targets)
     # the per-body theta rule with the learned policy's arithmetic (FP32 pairs, compensated)
     plain32 = []
-    for th in (0.3, 0.35, 0.4, 0.5):
+    for th in (0.3, 0.325, 0.35, 0.4, 0.5):
         tree.set_theta(th)
         ms = learned.timed(lambda: tree.accel(t["x"], t["y"], t["z"], *acc, G, learned.EPS2,
                                               "theta", "f32c"))
