@@ -485,6 +485,15 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
                             "max": float(rel.max())},
         "arithmetic": "double-float (FP32 pairs, ~2^-46 per pair term) for the accepted "
                       "monopoles; FP64 for positions, opening decisions and the output"}
+    # the headline step replayed from a captured CUDA graph (one launch per step instead of 54
+    # kernel launches), on copies of the state
+    vel2 = [torch.zeros_like(p) for p in pos]
+    vh2 = [torch.zeros_like(p) for p in pos]
+    acc3 = [a.clone() for a in acc64]
+    g = tree.graph(m, pos2, vel2, vh2, acc3, G, EPS2, DT, 1, "theta", "f64")
+    ms = timed(g.launch, 10)
+    g.close()
+    out["bh_f64_theta0.5_1M_graph_step"] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms}
     # naive FP64 on the reference's CPU-path configuration (16,384-body disc)
     n = 16384
     dd = generators.heliocentric_disc(n, 1)

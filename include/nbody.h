@@ -262,6 +262,16 @@ nb_status nb_bh_tree_set_theta(nb_bh_tree* tree, double theta);
 nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* tree, const double* m, const double* x,
                       const double* y, const double* z, uint32_t n, double G,
                       nb_stream_t stream);
+/* Captures `steps` Barnes-Hut leapfrog steps (kick-drift, nb_bh_build, nb_bh_accel with the
+ * given opening rule and precision, kick) of n bodies into a CUDA graph; nb_graph_launch replays
+ * them (one launch for all of a step's kernels), nb_graph_destroy frees it. The arrays, the tree
+ * and its policy are bound at capture time. Phase timing must be off. */
+nb_status nb_bh_graph_create(nb_ctx* ctx, nb_bh_tree* tree, const double* m, double* x, double* y,
+                             double* z, double* vx, double* vy, double* vz, double* vhx,
+                             double* vhy, double* vhz, double* ax, double* ay, double* az,
+                             uint32_t n, double G, double eps2, double dt, int steps,
+                             nb_opening opening, nb_precision prec, nb_graph** out);
+
 /* Phase timing of nb_bh_build (for measurements): when enabled, each build records CUDA events at
  * its phase boundaries; nb_bh_build_phase_ms (synchronous) returns the last build's durations
  * in ms: [0] AABB, [1] keys, [2] radix sort, [3] cells (runs, splits, counts, scan, emit),

@@ -27,11 +27,6 @@ struct nb_batch {
     nbpair::Plan plan{};
 };
 
-struct nb_graph {
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    int steps = 0;
-};
 
 namespace {
 
@@ -263,8 +258,14 @@ nb_status nb_batch_graph_create(nb_ctx* ctx, nb_batch* b, const double* m, doubl
             st = nb_leapfrog_kick(ctx, vx, vy, vz, vhx, vhy, vhz, ax, ay, az, b->n_total, dt,
                                   (nb_stream_t)s);
     }
+    return nb_finish_capture(s, st, steps, out);
+}
+
+}  // extern "C"
+
+nb_status nb_finish_capture(cudaStream_t s, nb_status st, int steps, nb_graph** out) {
     cudaGraph_t graph = nullptr;
-    e = cudaStreamEndCapture(s, &graph);
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
     cudaStreamDestroy(s);
     if (st != NB_OK) {
         if (graph) cudaGraphDestroy(graph);
@@ -284,6 +285,8 @@ nb_status nb_batch_graph_create(nb_ctx* ctx, nb_batch* b, const double* m, doubl
     *out = g;
     return NB_OK;
 }
+
+extern "C" {
 
 nb_status nb_graph_launch(nb_graph* g, nb_stream_t stream) {
     if (!g) return nb::set_error(NB_ERR_INVALID_ARG, "nb_graph_launch: null graph");

@@ -563,18 +563,29 @@ bh_count_kernel(const NodeRec64* __restrict__ rec, const uint32_t* __restrict__ 
 // walk (bh_theta_f64_kernel). Both produce identical results; the switch exists for comparison.
 int g_lockstep = 0;
 
-// Persistent launch of bh_theta_lane_kernel: resident blocks only, groups from work[1].
+// Resident blocks per SM of the two lane-kernel instantiations (queried once, before any
+// stream capture uses them).
+int g_lane_per_sm[2] = {0, 0};
+
 template <int MODE>
-nb_status launch_lane(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const double* y,
-                      const double* z, double* ax, double* ay, double* az, double G, double eps2,
-                      cudaStream_t s) {
-    static int per_sm[2] = {0, 0};
-    int& ps = per_sm[MODE == IEEE64 ? 0 : 1];
+nb_status lane_per_sm(int* out) {
+    int& ps = g_lane_per_sm[MODE == IEEE64 ? 0 : 1];
     if (ps == 0) {
         NB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, bh_theta_lane_kernel<MODE>,
                                                                   TR_THREADS, 0));
         if (ps < 1) ps = 1;
     }
+    *out = ps;
+    return NB_OK;
+}
+
+// Persistent launch of bh_theta_lane_kernel: resident blocks only, groups from work[1].
+template <int MODE>
+nb_status launch_lane(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const double* y,
+                      const double* z, double* ax, double* ay, double* az, double G, double eps2,
+                      cudaStream_t s) {
+    int ps = 0;
+    NB_TRY(lane_per_sm<MODE>(&ps));
     int grid = nb::ceil_div(t->n, TR_THREADS);
     if (grid > ctx->sm_count * ps) grid = ctx->sm_count * ps;
     NB_CUDA_TRY(cudaMemsetAsync(t->work + 1, 0, sizeof(uint32_t), s));
@@ -698,6 +709,38 @@ nb_status nb_bh_accel_learned_counted(nb_ctx* ctx, const nb_bh_tree* t, const do
     if (!counters_dev) return nb::set_error(NB_ERR_INVALID_ARG, "null counters");
     NB_CUDA_TRY(cudaMemsetAsync(counters_dev, 0, 2 * sizeof(unsigned long long), (cudaStream_t)stream));
     return nb::launch_learned(ctx, t, x, y, z, ax, ay, az, eps2, counters_dev, (cudaStream_t)stream);
+}
+
+nb_status nb_bh_graph_create(nb_ctx* ctx, nb_bh_tree* t, const double* m, double* x, double* y,
+                             double* z, double* vx, double* vy, double* vz, double* vhx,
+                             double* vhy, double* vhz, double* ax, double* ay, double* az,
+                             uint32_t n, double G, double eps2, double dt, int steps,
+                             nb_opening opening, nb_precision prec, nb_graph** out) {
+    NB_CHECK_CTX(ctx);
+    if (!t || !out || steps < 1)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_graph_create: bad arguments");
+    if (t->phase_timing)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_graph_create: phase timing is on");
+    *out = nullptr;
+    int ps = 0;  // one-time queries happen here, outside the capture
+    NB_TRY(lane_per_sm<IEEE64>(&ps));
+    NB_TRY(lane_per_sm<FAST64>(&ps));
+    cudaStream_t s;
+    NB_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        return nb::cuda_error(e, "cudaStreamBeginCapture");
+    }
+    nb_status st = NB_OK;
+    const nb_stream_t ns = (nb_stream_t)s;
+    for (int k = 0; k < steps && st == NB_OK; ++k) {
+        st = nb_leapfrog_kick_drift(ctx, vhx, vhy, vhz, vx, vy, vz, x, y, z, ax, ay, az, n, dt, ns);
+        if (st == NB_OK) st = nb_bh_build(ctx, t, m, x, y, z, n, G, ns);
+        if (st == NB_OK) st = nb_bh_accel(ctx, t, x, y, z, ax, ay, az, G, eps2, opening, prec, ns);
+        if (st == NB_OK) st = nb_leapfrog_kick(ctx, vx, vy, vz, vhx, vhy, vhz, ax, ay, az, n, dt, ns);
+    }
+    return nb_finish_capture(s, st, steps, out);
 }
 
 }  // extern "C"

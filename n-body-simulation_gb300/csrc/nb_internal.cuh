@@ -31,6 +31,17 @@ enum nb_scratch_slot : int {
     NB_SCRATCH_COUNT = 8,
 };
 
+// An instantiated CUDA graph of captured steps (nb_batch_graph_create, nb_bh_graph_create).
+struct nb_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int steps = 0;
+};
+
+// Ends a capture on stream s (begun by the caller), instantiates the graph and wraps it; on any
+// earlier failure (st != NB_OK) it only cleans up. Destroys s.
+nb_status nb_finish_capture(cudaStream_t s, nb_status st, int steps, nb_graph** out);
+
 struct nb_ctx {
     int device = 0;
     int sm_count = 0;

@@ -221,6 +221,7 @@ SIGNATURES.update({
     "nb_naive_accel_targets": [_vp] + [_vp] * 4 + [_u32, _vp, _u32] + [_vp] * 3 + [_d, _d, _vp],
     "nb_bh_set_policy": [_vp, _vp, C.c_float, _d, _u32, _u32],
     "nb_bh_set_phase_timing": [_vp, _i],
+    "nb_bh_graph_create": [_vp, _vp] + [_vp] * 13 + [_u32, _d, _d, _d, _i, _i, _i, _vp],
     "nb_bh_build_phase_ms": [_vp, _vp],
     "nb_bh_accel_learned_counted": [_vp, _vp] + [_vp] * 6 + [_d, _vp, _vp],
 })
@@ -262,6 +263,15 @@ class BHTree:
     def build(self, m, x, y, z, G, stream=None):
         check(self.lib.nb_bh_build(self.ctx.handle, self.handle, ptr(m), ptr(x), ptr(y), ptr(z),
                                    m.numel(), G, stream_ptr(stream)))
+
+    def graph(self, m, pos, vel, vh, acc, G, eps2, dt, steps, opening="theta", precision="f64"):
+        """CUDA graph of `steps` leapfrog steps (kick-drift, build, traversal, kick)."""
+        h = _vp()
+        check(self.lib.nb_bh_graph_create(self.ctx.handle, self.handle, ptr(m), *map(ptr, pos),
+                                          *map(ptr, vel), *map(ptr, vh), *map(ptr, acc),
+                                          m.numel(), G, eps2, dt, steps, OPENINGS[opening],
+                                          PRECISIONS[precision], C.byref(h)))
+        return Graph(h)
 
     def set_phase_timing(self, enable=True):
         check(self.lib.nb_bh_set_phase_timing(self.handle, 1 if enable else 0))

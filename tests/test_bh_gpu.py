@@ -265,3 +265,38 @@ def test_build_phase_timing(ctx):
     assert len(ms) == 5 and all(v > 0 for v in ms)
     assert sum(ms) <= total * 1.05 + 0.05
     tree.set_phase_timing(False)
+
+
+@pytest.mark.parametrize("precision", ["f64_ieee", "f64"])
+def test_graph_replay_equals_stepwise_steps(ctx, precision):
+    """A captured graph of K Barnes-Hut leapfrog steps gives the stepwise calls' state bit for
+    bit."""
+    import torch
+    from nbody.lib import BHTree
+    d = bodies("disc", 5000, seed=31)
+    n, dt, steps = 5000, 1.0 / 24, 3
+
+    def state():
+        s = {k: dev(d[k]) for k in ("m", "x", "y", "z", "vx", "vy", "vz")}
+        s["acc"] = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+        s["vh"] = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+        return s
+
+    A, B = state(), state()
+    ta, tb = BHTree(ctx, n, theta=0.5), BHTree(ctx, n, theta=0.5)
+    for s, t in ((A, ta), (B, tb)):
+        t.build(s["m"], s["x"], s["y"], s["z"], d["G"])
+        t.accel(s["x"], s["y"], s["z"], *s["acc"], d["G"], 1e-22, "theta", precision)
+    posA, velA = [A["x"], A["y"], A["z"]], [A["vx"], A["vy"], A["vz"]]
+    for _ in range(steps):
+        ctx.kick_drift(A["vh"], velA, posA, A["acc"], dt)
+        ta.build(A["m"], *posA, d["G"])
+        ta.accel(*posA, *A["acc"], d["G"], 1e-22, "theta", precision)
+        ctx.kick(velA, A["vh"], A["acc"], dt)
+    g = tb.graph(B["m"], [B["x"], B["y"], B["z"]], [B["vx"], B["vy"], B["vz"]], B["vh"],
+                 B["acc"], d["G"], 1e-22, dt, steps, "theta", precision)
+    g.launch()
+    ctx.sync()
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(host(A[k]), host(B[k]))
+    g.close()
