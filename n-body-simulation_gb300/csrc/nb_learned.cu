@@ -321,8 +321,19 @@ constexpr uint32_t LT_DIRECT = 8;   // opened cells up to this many bodies: dire
 constexpr int LT_LIST = 384;        // interaction list entries per warp (a full step fits)
 static_assert(LT_LIST >= LT_BATCH * (LT_DIRECT + 1), "one step must fit in an empty list");
 
-// Sum of the interactions in list[0..count) for one body; 4 independent accumulators. An entry
-// at zero distance (the body itself) contributes nothing.
+// Sum of the interactions in list[0..count) for one body; 4 independent accumulators. 1/r is
+// capped at 1e12: an entry at zero distance (the body itself) then contributes exactly 0 even
+// without softening, and with eps^2 >= 1e-24 the cap never binds.
+__device__ __forceinline__ void pair_term(const float4 e, float px, float py, float pz,
+                                          float eps2, float& ax, float& ay, float& az) {
+    const float dx = e.x - px, dy = e.y - py, dz = e.z - pz;
+    const float inv = fminf(nb_rsqrt_f32(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)))), 1e12f);
+    const float w = e.w * inv * inv * inv;
+    ax = fmaf(dx, w, ax);
+    ay = fmaf(dy, w, ay);
+    az = fmaf(dz, w, az);
+}
+
 __device__ __forceinline__ void flush_list(const float4* __restrict__ list, int count, float px,
                                            float py, float pz, float eps2, float& ox, float& oy,
                                            float& oz) {
@@ -330,27 +341,9 @@ __device__ __forceinline__ void flush_list(const float4* __restrict__ list, int 
     int j = 0;
     for (; j + 4 <= count; j += 4) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const float4 e = list[j + u];
-            const float dx = e.x - px, dy = e.y - py, dz = e.z - pz;
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const float inv = rsqrtf(r2 + eps2);
-            const float w = r2 > 0.f ? e.w * inv * inv * inv : 0.f;
-            ax[u] = fmaf(dx, w, ax[u]);
-            ay[u] = fmaf(dy, w, ay[u]);
-            az[u] = fmaf(dz, w, az[u]);
-        }
+        for (int u = 0; u < 4; ++u) pair_term(list[j + u], px, py, pz, eps2, ax[u], ay[u], az[u]);
     }
-    for (; j < count; ++j) {
-        const float4 e = list[j];
-        const float dx = e.x - px, dy = e.y - py, dz = e.z - pz;
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float inv = rsqrtf(r2 + eps2);
-        const float w = r2 > 0.f ? e.w * inv * inv * inv : 0.f;
-        ax[0] = fmaf(dx, w, ax[0]);
-        ay[0] = fmaf(dy, w, ay[0]);
-        az[0] = fmaf(dz, w, az[0]);
-    }
+    for (; j < count; ++j) pair_term(list[j], px, py, pz, eps2, ax[0], ay[0], az[0]);
     ox = (ax[0] + ax[1]) + (ax[2] + ax[3]);
     oy = (ay[0] + ay[1]) + (ay[2] + ay[3]);
     oz = (az[0] + az[1]) + (az[2] + az[3]);
@@ -382,7 +375,8 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
                   uint32_t* __restrict__ next_group) {
     __shared__ uint32_t stack[LT_WARPS][LT_CAP];
     __shared__ __align__(16) __nv_bfloat16 feat[LT_WARPS][LT_BATCH][16];
-    __shared__ float4 gpos[LT_WARPS][32];
+    // the group's positions as packed pairs (bodies 2j, 2j+1) per axis, for the gap loop
+    __shared__ nb_f2 gpx[LT_WARPS][16], gpy[LT_WARPS][16], gpz[LT_WARPS][16];
     __shared__ float4 ilist[LT_WARPS][LT_LIST];
     __shared__ uint32_t wfrag[MF_W * 32];
     __shared__ float bfrag[MF_B * 32];
@@ -418,7 +412,9 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
                     pz = (ph.z - ghz) + (pl.z - glz);
         const GroupGeo G = group_geo(valid, ph.x, ph.y, ph.z, a_prev);
         const float inf = __int_as_float(0x7f800000);
-        gpos[wi][lane] = valid ? make_float4(ph.x, ph.y, ph.z, 0.f) : make_float4(inf, inf, inf, 0.f);
+        reinterpret_cast<float*>(gpx[wi])[lane] = valid ? ph.x : inf;
+        reinterpret_cast<float*>(gpy[wi])[lane] = valid ? ph.y : inf;
+        reinterpret_cast<float*>(gpz[wi])[lane] = valid ? ph.z : inf;
         const bool use_net = params != nullptr;
         const MlpFragsSmem F{wfrag, bfrag, lane};
         uint32_t* st = stack[wi];
@@ -464,12 +460,16 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
                 ++n_steps;
             }
             float m2 = inf;
-            if (live) {
+            if (live) {  // packed: two group bodies per f32x2 operation
+                const nb_f2 cx2 = f2_pack(r.cx, r.cx), cy2 = f2_pack(r.cy, r.cy),
+                            cz2 = f2_pack(r.cz, r.cz);
     #pragma unroll 8
-                for (int j = 0; j < 32; ++j) {
-                    const float4 q = gpos[wi][j];
-                    const float dx = r.cx - q.x, dy = r.cy - q.y, dz = r.cz - q.z;
-                    m2 = fminf(m2, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                for (int j = 0; j < 16; ++j) {
+                    const nb_f2 dx = f2_sub(gpx[wi][j], cx2), dy = f2_sub(gpy[wi][j], cy2),
+                                dz = f2_sub(gpz[wi][j], cz2);
+                    float d0, d1;
+                    f2_unpack(f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz))), d0, d1);
+                    m2 = fminf(m2, fminf(d0, d1));
                 }
             }
             const float gap = sqrtf(m2);
