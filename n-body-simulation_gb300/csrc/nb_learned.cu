@@ -29,8 +29,7 @@ constexpr int NF = 8;
 constexpr float SQRT3 = 1.7320508f;
 
 struct GroupGeo {
-    float cx, cy, cz, r, a_ref, lg_aref;  // lg_aref = log2(a_ref)
-    float hx, hy, hz;  // half extents of the group's bounding box
+    float cx, cy, cz, r, a_ref, lg_aref;  // box centre, radius, weakest |a|, log2(a_ref)
 };
 
 __device__ __forceinline__ float warp_min(float v) {
@@ -53,9 +52,6 @@ __device__ GroupGeo group_geo(bool valid, float px, float py, float pz, float a_
     g.cx = 0.5f * (lx + hx);
     g.cy = 0.5f * (ly + hy);
     g.cz = 0.5f * (lz + hz);
-    g.hx = 0.5f * (hx - lx);
-    g.hy = 0.5f * (hy - ly);
-    g.hz = 0.5f * (hz - lz);
     const float dx = px - g.cx, dy = py - g.cy, dz = pz - g.cz;
     g.r = warp_max(valid ? sqrtf(dx * dx + dy * dy + dz * dz) : 0.f);
     g.a_ref = fmaxf(warp_min(valid ? a_prev : inf), 1e-30f);
