@@ -601,6 +601,7 @@ namespace nb {
 nb_status launch_learned(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const double* y,
                          const double* z, double* ax, double* ay, double* az, double eps2,
                          unsigned long long* counters, cudaStream_t s);
+nb_status learned_per_sm(int* out);
 }
 
 extern "C" {
@@ -725,6 +726,7 @@ nb_status nb_bh_graph_create(nb_ctx* ctx, nb_bh_tree* t, const double* m, double
     int ps = 0;  // one-time queries happen here, outside the capture
     NB_TRY(lane_per_sm<IEEE64>(&ps));
     NB_TRY(lane_per_sm<FAST64>(&ps));
+    NB_TRY(nb::learned_per_sm(&ps));
     cudaStream_t s;
     NB_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);

@@ -983,6 +983,19 @@ nb_status nb_bh_generate_pairs(nb_ctx* ctx, const nb_bh_tree* t, const double* m
 
 namespace nb {
 
+// Resident blocks per SM of the learned traversal (queried once; also called before stream
+// captures so that no query happens inside one).
+nb_status learned_per_sm(int* out) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        NB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bh_learned_kernel<false>,
+                                                                  LT_THREADS, 0));
+        if (per_sm < 1) per_sm = 1;
+    }
+    *out = per_sm;
+    return NB_OK;
+}
+
 nb_status launch_learned(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const double* y,
                          const double* z, double* ax, double* ay, double* az, double eps2,
                          unsigned long long* counters, cudaStream_t s) {
@@ -990,7 +1003,9 @@ nb_status launch_learned(nb_ctx* ctx, const nb_bh_tree* t, const double* x, cons
         return set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: NB_OPEN_LEARNED needs nb_bh_set_policy");
     const uint32_t warps = (t->n + 31) / 32;
     int blocks = ceil_div(warps, LT_WARPS);
-    if (blocks > ctx->sm_count * 4) blocks = ctx->sm_count * 4;  // 4 resident blocks per SM
+    int per_sm = 0;
+    NB_TRY(learned_per_sm(&per_sm));
+    if (blocks > ctx->sm_count * per_sm) blocks = ctx->sm_count * per_sm;
     NB_CUDA_TRY(cudaMemsetAsync(t->work, 0, sizeof(uint32_t), s));
     auto kernel = counters ? bh_learned_kernel<true> : bh_learned_kernel<false>;
     kernel<<<blocks, LT_THREADS, 0, s>>>(
