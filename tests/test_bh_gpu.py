@@ -300,3 +300,26 @@ def test_graph_replay_equals_stepwise_steps(ctx, precision):
     for k in ("x", "y", "z", "vx", "vy", "vz"):
         np.testing.assert_array_equal(host(A[k]), host(B[k]))
     g.close()
+
+
+def test_graph_create_rejects_phase_timing_and_bad_steps(ctx):
+    import torch
+    from nbody.lib import BHTree, NBodyError
+    d = bodies("plummer", 500, seed=3)
+    n = 500
+    t = BHTree(ctx, n, theta=0.5)
+    s = {k: dev(d[k]) for k in ("m", "x", "y", "z", "vx", "vy", "vz")}
+    z = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(6)]
+    args = (s["m"], [s["x"], s["y"], s["z"]], [s["vx"], s["vy"], s["vz"]], z[:3], z[3:], 1.0,
+            1e-6, 1e-3)
+    with pytest.raises(NBodyError, match="INVALID_ARG"):
+        t.graph(*args, 0)
+    t.set_phase_timing(True)
+    with pytest.raises(NBodyError, match="phase timing"):
+        t.graph(*args, 1)
+    t.set_phase_timing(False)
+    g = t.graph(*args, 2, "theta", "df64")
+    g.launch()
+    ctx.sync()
+    g.close()
+    t.close()

@@ -97,7 +97,7 @@ def test_range_matches_full(ctx):
     import torch
     d = bodies("plummer", 3000, seed=2)
     t = {k: dev(d[k]) for k in ("m", "x", "y", "z")}
-    for prec in ("f64_ieee", "f32c"):
+    for prec in ("f64_ieee", "f32c", "df64"):
         full = run_naive(ctx, d, 1e-6, prec)
         ax, ay, az = (torch.zeros(3000, dtype=torch.float64, device="cuda") for _ in range(3))
         ctx.naive_accel_range(t["m"], t["x"], t["y"], t["z"], ax, ay, az, 1000, 2100, 1.0, 1e-6,
@@ -106,6 +106,8 @@ def test_range_matches_full(ctx):
         part = host(ax)
         if prec == "f64_ieee":
             np.testing.assert_array_equal(part[1000:2100], full[0][1000:2100])
+        elif prec == "df64":
+            np.testing.assert_allclose(part[1000:2100], full[0][1000:2100], rtol=1e-12, atol=1e-15)
         else:
             np.testing.assert_allclose(part[1000:2100], full[0][1000:2100], rtol=1e-5, atol=1e-9)
         assert np.all(part[:1000] == 0) and np.all(part[2100:] == 0)
