@@ -29,24 +29,50 @@ namespace {
 constexpr int BH_THREADS = 256;
 constexpr uint32_t RUN_LIMIT = 1u << 14;  // longest run of equal first key words we re-sort
 
-// Octant digits of levels [word*21, word*21+21) for a body (FP64 recurrence, no contraction).
+// Order-preserving map of an FP64 value (no NaN, -0 already turned into +0) to uint64: the
+// strict comparisons of the recurrence become integer comparisons (ALU instead of FP64 pipe).
+__device__ __forceinline__ uint64_t ordered_bits(double v) {
+    const uint64_t u = (uint64_t)__double_as_longlong(v);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// Octant digits of levels [word*21, word*21+21) for a body: the reference's FP64 recurrence
+// (mid = min + edge/2 rounded as FP64, strict compares, child min = mid or min). Only the three
+// midpoint additions per level run on the FP64 pipe: the compares are integer compares of
+// order-preserving bit patterns (exact: a midpoint is never -0 since edge/2 > 0, and the body's
+// -0 coordinates are taken as +0, which compares equal), and edge/2 is an exponent decrement
+// (exact for the normal, positive edges of <= 42 levels).
 __device__ uint64_t key_word(const double* __restrict__ box, double px, double py, double pz,
                              int word) {
     double mnx = box[0], mny = box[1], mnz = box[2], e = box[6];
+    uint64_t e_bits = (uint64_t)__double_as_longlong(e);
+    // exponent decrements stay exact while the edge is positive and normal after 42 halvings;
+    // otherwise (a zero or tiny box) the halving is an FP64 multiply
+    const bool halve_bits = (e_bits >> 52) > 64 && (e_bits >> 52) < 0x7ff;
+    const uint64_t ox = ordered_bits(px == 0.0 ? 0.0 : px), oy = ordered_bits(py == 0.0 ? 0.0 : py),
+                   oz = ordered_bits(pz == 0.0 ? 0.0 : pz);
     uint64_t key = 0;
     const int first = word * NB_KEY_LEVELS, last = first + NB_KEY_LEVELS;
     for (int L = 0; L < last; ++L) {
-        const double ce = e / 2;
+        double ce;
+        if (halve_bits) {
+            e_bits -= 1ull << 52;  // edge / 2
+            ce = __longlong_as_double((long long)e_bits);
+        } else {
+            ce = e / 2;
+            e = ce;
+        }
         const double midx = __dadd_rn(mnx, ce);
         const double midy = __dadd_rn(mny, ce);
         const double midz = __dadd_rn(mnz, ce);
-        const bool up = py > midy, rt = px > midx, bk = pz < midz;
+        const bool up = oy > ordered_bits(midy), rt = ox > ordered_bits(midx),
+                   bk = oz < ordered_bits(midz);
         if (L >= first)
-            key = (key << 3) | nb_visit_of_octant((uint32_t)up * 4u + (uint32_t)rt * 2u + (uint32_t)bk);
+            key = (key << 3) |
+                  nb_visit_of_octant((uint32_t)up * 4u + (uint32_t)rt * 2u + (uint32_t)bk);
         if (rt) mnx = midx;
         if (up) mny = midy;
         if (!bk) mnz = midz;
-        e = ce;
     }
     return key;
 }
