@@ -16,6 +16,8 @@
 //     an exclusive scan gives every node its DFS pre-order index and skip link.
 //  7. bottom-up centre of mass: the last child to finish a cell sums the cell's children in
 //     octant order 0..7 (bit-identical to BarnesHutOctree.cpp:304-311).
+#include <cuda/atomic>
+
 #include "nb_bh.cuh"
 #include "nb_sort.cuh"
 
@@ -376,9 +378,10 @@ __global__ void com_kernel(ComArgs A) {
                                  (float)(rz - (double)hz), 0.f);
     uint32_t cur = A.node_parent[idx];
     while (cur != NB_NONE) {
-        __threadfence();
-        if (atomicAdd(&A.node_arrive[cur], 1u) != A.node_nchild[cur] - 1u) return;
-        __threadfence();
+        // acquire-release arrival: publishes this child's sums and, for the last child, makes
+        // the siblings' sums visible (one device-scope RMW instead of two full fences)
+        cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrive(A.node_arrive[cur]);
+        if (arrive.fetch_add(1u, cuda::memory_order_acq_rel) != A.node_nchild[cur] - 1u) return;
         // children by visit rank (written by emit_kernel); rewritten below as the compacted
         // visit-order list the learned traversal reads
         uint4* cl = reinterpret_cast<uint4*>(A.children + (size_t)cur * 8);
