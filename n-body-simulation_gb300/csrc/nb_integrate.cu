@@ -260,13 +260,41 @@ aabb_kernel(const double* __restrict__ x, const double* __restrict__ y,
         last = (done == gridDim.x - 1);
     }
     __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        MinMax6 r = part[0];
-        for (uint32_t b = 1; b < gridDim.x; ++b)
+    if (!last) return;
+    // the last block reduces all blocks' partials with all its threads
+    __threadfence();
+    for (int a = 0; a < 3; ++a) {
+        mn[a] = zero;
+        mx[a] = zero;
+    }
+    for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+        const MinMax6 q = part[b];
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = min(mn[a], q.v[a]);
+            mx[a] = max(mx[a], q.v[3 + a]);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        for (int off = 16; off > 0; off >>= 1) {
+            mn[a] = min(mn[a], __shfl_down_sync(0xffffffffu, mn[a], off));
+            mx[a] = max(mx[a], __shfl_down_sync(0xffffffffu, mx[a], off));
+        }
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        for (int a = 0; a < 3; ++a) {
+            warp_part[threadIdx.x >> 5].v[a] = mn[a];
+            warp_part[threadIdx.x >> 5].v[3 + a] = mx[a];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        MinMax6 r = warp_part[0];
+        for (int w = 1; w < AABB_THREADS / 32; ++w)
             for (int a = 0; a < 3; ++a) {
-                r.v[a] = min(r.v[a], part[b].v[a]);
-                r.v[3 + a] = max(r.v[3 + a], part[b].v[3 + a]);
+                r.v[a] = min(r.v[a], warp_part[w].v[a]);
+                r.v[3 + a] = max(r.v[3 + a], warp_part[w].v[3 + a]);
             }
         cube_rule(val_of(r.v[0]), val_of(r.v[1]), val_of(r.v[2]), val_of(r.v[3]),
                   val_of(r.v[4]), val_of(r.v[5]), out);
