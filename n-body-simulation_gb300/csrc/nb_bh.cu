@@ -344,8 +344,13 @@ __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double 
         const double ox = A.box[0] + A.box[6] / 2, oy = A.box[1] + A.box[6] / 2,
                      oz = A.box[2] + A.box[6] / 2;
         const double gx = r.cx - ox, gy = r.cy - oy, gz = r.cz - oz;
-        const double s2 = qsum / sm - (gx * gx + gy * gy + gz * gz);
-        x.spread = (float)sqrt(s2 > 0 ? s2 : 0.0);
+        // 1/M from the hardware estimate and one Newton step (~2^-44: the spread is a feature of
+        // the learned policy, not a sum of the reference), the root in FP32
+        double inv;
+        asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(inv) : "d"(sm));
+        inv = inv * fma(-sm, inv, 2.0);
+        const double s2 = qsum * inv - (gx * gx + gy * gy + gz * gz);
+        x.spread = sqrtf((float)(s2 > 0 ? s2 : 0.0));
     } else {
         x.spread = 0.f;
     }
