@@ -368,7 +368,7 @@ def run_ours(args):
     e2e_value = ws * e2e_steps / t_e2e
 
     also = {}
-    if rank == 0 and not args.quick:
+    if rank == 0 and ws == 1 and not args.quick:  # one GPU only: replicas runs stay short
         also = secondary_measurements(ctx, tree, m, pos, acc, G)
 
     cpu = None
