@@ -28,6 +28,7 @@ enum nb_scratch_slot : int {
     NB_SCRATCH_AABB = 2,        // per-block partial min/max
     NB_SCRATCH_LABELS = 3,      // sampled (group, cell) pairs of the label generator
     NB_SCRATCH_NAIVE_DF = 4,    // triple-float sources of the double-float pair kernel
+    NB_SCRATCH_PAIR_SYM = 5,    // sources and partials of the symmetric FP32 pair kernel
     NB_SCRATCH_COUNT = 8,
 };
 

@@ -7,12 +7,15 @@
 //    FP64 evaluation of NaiveAlgorithm.cpp:331-351.
 //  * NB_F64: same loop with FMAs and m (r^2 + eps^2)^(-3/2) from the hardware rsqrt estimate with
 //    one correction (nb_m_rinv3_f64; FP64-pipe bound on GB300).
-//  * NB_F32C: the FP32-compensated pair kernel of nb_pair.cuh (scalar FP32 pair math, TwoSum
-//    accumulation, stream-K persistent CTAs, cp.async.bulk j-tiles behind bounded mbarrier
-//    waits), run as a batch of one system.
+//  * NB_F32C: over all bodies of a large system, the symmetric FP32 pair kernel of
+//    nb_pair_sym.cu (each unordered pair once, added to both bodies); otherwise (target ranges,
+//    small systems) the one-sided FP32-compensated pair kernel of nb_pair.cuh (scalar FP32 pair
+//    math, TwoSum accumulation, stream-K persistent CTAs, cp.async.bulk j-tiles behind bounded
+//    mbarrier waits), run as a batch of one system.
 //  * NB_DF64: double-float pair math on the FP32 pipe (FP64-accurate to ~1e-14).
 #include "nb_internal.cuh"
 #include "nb_pair.cuh"
+#include "nb_pair_sym.cuh"
 
 namespace {
 
@@ -180,11 +183,44 @@ naive_f64_targets_kernel(const double* __restrict__ m, const double* __restrict_
 // targets are [i_begin, i_end).
 // ---------------------------------------------------------------------------------------------
 int g_naive_pair_cfg = 0;  // tile configuration (nb_naive_set_pair_config)
+// Symmetric kernel (nb_pair_sym.cu) for full target ranges (nb_naive_set_symmetric): mode 0
+// never, 1 automatic, 2 always; and its configuration.
+int g_naive_sym_mode = 1;
+int g_naive_sym_cfg = 0;
+// Automatic selection wants at least this many units per persistent CTA (the one-sided kernel
+// spreads small systems better) and j-side partials (12 bytes per unit and tile body, about
+// 6 n^2 / IB bytes in all) below the cap.
+constexpr uint64_t SYM_MIN_UNITS_PER_CTA = 8;
+constexpr size_t SYM_PART_CAP_BYTES = (size_t)4 << 30;
+
+nb_status naive_f32c_sym(nb_ctx* ctx, int cfg, const nbsym::SymPlan& S, const double* m,
+                         const double* x, const double* y, const double* z, double* ax,
+                         double* ay, double* az, double G, double eps2, cudaStream_t stream) {
+    const size_t src_bytes = (nb::sym_src_bytes(cfg, S) + 255) & ~(size_t)255;
+    const size_t pi_bytes = (nb::sym_part_i_floats(cfg, S) * sizeof(float) + 255) & ~(size_t)255;
+    const size_t pj_bytes = nb::sym_part_j_floats(cfg, S) * sizeof(float);
+    void* base = nullptr;
+    NB_TRY(nb::scratch(ctx, NB_SCRATCH_PAIR_SYM, src_bytes + pi_bytes + pj_bytes, &base));
+    char* b = (char*)base;
+    return nb::sym_launch(cfg, S, m, x, y, z, G, eps2, (float4*)b, (float*)(b + src_bytes),
+                          (float*)(b + src_bytes + pi_bytes), ax, ay, az, ctx->dev_error, stream);
+}
 
 nb_status naive_f32c(nb_ctx* ctx, const double* m, const double* x, const double* y,
                      const double* z, double* ax, double* ay, double* az, uint32_t n,
                      uint32_t i_begin, uint32_t i_end, double G, double eps2,
                      cudaStream_t stream) {
+    if (i_begin == 0 && i_end == n && g_naive_sym_mode != 0) {
+        const int scfg = g_naive_sym_cfg;
+        int sym_per_sm = 0;
+        NB_TRY(nb::sym_ctas_per_sm(scfg, &sym_per_sm));
+        const nbsym::SymPlan S = nb::sym_plan(scfg, n, (uint32_t)(ctx->sm_count * sym_per_sm));
+        const bool use =
+            g_naive_sym_mode == 2 ||
+            (S.units >= SYM_MIN_UNITS_PER_CTA * S.ctas &&
+             nb::sym_part_j_floats(scfg, S) * sizeof(float) <= SYM_PART_CAP_BYTES);
+        if (use) return naive_f32c_sym(ctx, scfg, S, m, x, y, z, ax, ay, az, G, eps2, stream);
+    }
     const int cfg = g_naive_pair_cfg;
     const nb::PairConfig& C = nb::kPairConfigs[cfg];
     int per_sm = 0;
@@ -437,6 +473,16 @@ nb_status nb_naive_set_pair_config(int config) {
     if (config < 0 || config >= nb::NB_PAIR_CONFIGS)
         return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_set_pair_config: config %d", config);
     g_naive_pair_cfg = config;
+    return NB_OK;
+}
+
+nb_status nb_naive_set_symmetric(int mode, int config) {
+    if (mode < 0 || mode > 2)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_set_symmetric: mode %d", mode);
+    if (config < 0 || config >= nb::NB_SYM_CONFIGS)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_set_symmetric: config %d", config);
+    g_naive_sym_mode = mode;
+    g_naive_sym_cfg = config;
     return NB_OK;
 }
 

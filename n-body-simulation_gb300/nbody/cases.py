@@ -2,7 +2,10 @@
 
     python n-body-simulation_gb300/nbody/cases.py pair [N] [config]
         seeded Plummer sphere (G = M = a = 1, softening 1e-3), three FP32-compensated naive
-        evaluations (pair_f32c_kernel) with tile configuration `config`
+        evaluations with the one-sided kernel (pair_f32c_kernel), tile configuration `config`
+    python n-body-simulation_gb300/nbody/cases.py sym [N] [config]
+        the same three evaluations with the symmetric kernel (pair_sym_kernel), configuration
+        `config`
     python n-body-simulation_gb300/nbody/cases.py learned [N] [log10_tau] [pairs]
         seeded disc + Plummer mix: labelled pairs and a short training of the opening network,
         then three learned traversals (bh_learned_kernel) at threshold tau
@@ -22,13 +25,18 @@ import sys
 sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 
 
-def pair_case(n: int = 262144, config: int = 0):
+def pair_case(n: int = 262144, config: int = 0, symmetric: bool = False):
     import torch
 
     from nbody import generators, learned
-    from nbody.lib import Context, set_naive_pair_config
+    from nbody.lib import (SYM_ALWAYS, SYM_NEVER, Context, set_naive_pair_config,
+                           set_naive_symmetric)
     ctx = Context(0)
-    set_naive_pair_config(config)
+    if symmetric:
+        set_naive_symmetric(SYM_ALWAYS, config)
+    else:
+        set_naive_symmetric(SYM_NEVER, 0)
+        set_naive_pair_config(config)
     t = learned.device_system(generators.plummer(n, 1))
     acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
     for _ in range(3):
@@ -74,12 +82,13 @@ def df64_case(n: int = 262144):
 
 
 def main(argv):
-    if not argv or argv[0] not in ("pair", "learned", "df64"):
+    if not argv or argv[0] not in ("pair", "sym", "learned", "df64"):
         print(__doc__)
         return 2
     args = argv[1:]
-    if argv[0] == "pair":
-        pair_case(int(args[0]) if args else 262144, int(args[1]) if len(args) > 1 else 0)
+    if argv[0] in ("pair", "sym"):
+        pair_case(int(args[0]) if args else 262144, int(args[1]) if len(args) > 1 else 0,
+                  argv[0] == "sym")
     elif argv[0] == "df64":
         df64_case(int(args[0]) if args else 262144)
     else:

@@ -27,7 +27,8 @@ import time
 import numpy as np
 
 from . import generators, learned
-from .lib import Batch, BHTree, Context, fma_peak
+from .lib import (SYM_AUTO, SYM_NEVER, Batch, BHTree, Context, fma_peak,
+                  set_naive_symmetric)
 
 # nominal MUFU rate of one SM (reciprocal square roots per clock) and the GB300's SM count
 # and maximum SM clock: the SFU peak the pair kernels are reported against
@@ -79,6 +80,13 @@ def precision_form(ctx: Context, n: int = 262144, steps: int = 1000, dt: float =
     ctx.naive_accel_targets(t["m"], t["x"], t["y"], t["z"], tg, *ref, G, eps2)
     ctx.sync()
     ref = [v.cpu().numpy() for v in ref]
+    # the one-sided kernel (every ordered pair), then the default selection: at this size the
+    # symmetric kernel (each unordered pair once, added to both bodies)
+    set_naive_symmetric(SYM_NEVER)
+    ms32_one = _events_ms(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, G, eps2,
+                                                  "f32c"), 5)
+    med1, p991 = learned.errors(acc, ref, targets)
+    set_naive_symmetric(SYM_AUTO)
     ms32 = _events_ms(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, G, eps2,
                                               "f32c"), 5)
     med, p99 = learned.errors(acc, ref, targets)
@@ -122,12 +130,21 @@ def precision_form(ctx: Context, n: int = 262144, steps: int = 1000, dt: float =
     return {
         "workload": f"naive all-pairs, {n}-body Plummer sphere (G=M=a=1, seed {seed}), "
                     f"softening {softening}",
+        "f32c_kernel": "pair_sym_kernel (symmetric: each unordered pair evaluated once and "
+                       "added to both bodies; 20 flop per ordered pair counted, as for the "
+                       "one-sided kernel)",
         "f32c_ms_per_eval": ms32, "f64_ms_per_eval": ms64,
         "f32c_gpairs_per_s": gps32 / 1e9, "f64_gpairs_per_s": pairs / (ms64 * 1e-3) / 1e9,
         "f32c_frac_of_measured_fp32_fma_peak": gps32 * 20 / fp32_peak,
         "fp32_fma_peak_tflops_measured": fp32_peak / 1e12,
-        "f32c_frac_of_nominal_sfu_rsqrt_peak": gps32 / sfu_peak,
+        "f32c_rsqrt_per_s_frac_of_nominal_sfu_peak": gps32 / 2 / sfu_peak,
         "force_rel_err_vs_fp64": {"median": med, "p99": p99, "bodies": len(targets)},
+        "f32c_one_sided": {"kernel": "pair_f32c_kernel (every ordered pair)",
+                           "ms_per_eval": ms32_one,
+                           "gpairs_per_s": pairs / (ms32_one * 1e-3) / 1e9,
+                           "frac_of_measured_fp32_fma_peak":
+                               pairs / (ms32_one * 1e-3) * 20 / fp32_peak,
+                           "force_rel_err_vs_fp64": {"median": med1, "p99": p991}},
         "energy_drift_f32c": {"steps": steps, "dt": dt, "E0": e0[2], "E1": e1[2],
                               "rel": abs(e1[2] - e0[2]) / abs(e0[2]), "run_s": run_s},
         "f32c_vs_f64_max_position_diff": {"steps": fp64_steps, "value": dpos},
