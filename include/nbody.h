@@ -122,15 +122,21 @@ typedef struct nb_graph nb_graph;
 nb_status nb_batch_create(nb_ctx* ctx, uint32_t n_systems, const uint32_t* counts_host,
                           nb_batch** out);
 nb_status nb_batch_destroy(nb_batch* batch);
-/* Total bodies and the current tile configuration: CTA threads, targets per thread, j-tile. */
+/* Batch tile configurations: 0..NB_PAIR_CONFIG_COUNT-1 run the one-sided pair kernel (every
+ * ordered pair), NB_PAIR_CONFIG_COUNT.. NB_BATCH_CONFIG_COUNT-1 the symmetric kernel's shapes
+ * (each unordered pair once, added to both bodies; same order as nb_naive_set_symmetric). */
+#define NB_BATCH_CONFIG_COUNT 16
+/* Total bodies and the current tile configuration: CTA threads, targets (bodies) per thread,
+ * j-tile. */
 nb_status nb_batch_info(const nb_batch* batch, uint32_t* n_total, int* config, int* threads,
                         int* targets_per_thread, int* j_tile);
 nb_status nb_batch_set_config(nb_ctx* ctx, nb_batch* batch, int config);
 nb_status nb_batch_naive_accel(nb_ctx* ctx, nb_batch* batch, const double* m, const double* x,
                                const double* y, const double* z, double* ax, double* ay,
                                double* az, double G, double eps2, nb_stream_t stream);
-/* Autotuner (synchronous): times every tile configuration on these arrays (reps launches each,
- * CUDA events), keeps the fastest; ms_per_config (host, NB_PAIR_CONFIG_COUNT entries) optional. */
+/* Autotuner (synchronous): times every tile configuration of both kernels on these arrays (reps
+ * launches each, CUDA events), keeps the fastest; ms_per_config (host, NB_BATCH_CONFIG_COUNT
+ * entries) optional. */
 nb_status nb_batch_autotune(nb_ctx* ctx, nb_batch* batch, const double* m, const double* x,
                             const double* y, const double* z, double* ax, double* ay, double* az,
                             double G, double eps2, int reps, float* ms_per_config, int* chosen);

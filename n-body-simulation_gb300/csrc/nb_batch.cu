@@ -1,5 +1,6 @@
 // nb_batch.cu -- ensembles of independent systems of uneven size in one persistent launch
-// (nb_pair.cuh), the tile autotuner, and CUDA-graph capture of whole leapfrog steps.
+// (the one-sided kernel of nb_pair.cuh or the symmetric kernel of nb_pair_sym.cu), the tile
+// autotuner over both kernels' shapes, and CUDA-graph capture of whole leapfrog steps.
 //
 // All systems live in concatenated FP64 arrays; system s owns bodies [off_s, off_s + count_s).
 // Forces never cross systems. The batch pre-allocates every buffer its launches use (plan,
@@ -7,9 +8,18 @@
 // into a CUDA graph and replayed.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "nb_pair.cuh"
+#include "nb_pair_sym.cuh"
+
+namespace {
+// Batch configurations: 0 .. NB_PAIR_CONFIGS-1 the one-sided pair kernel's tile shapes, then
+// NB_SYM_CONFIGS shapes of the symmetric kernel (each unordered pair once, both bodies).
+constexpr int NB_BATCH_CONFIGS = nb::NB_PAIR_CONFIGS + nb::NB_SYM_CONFIGS;
+inline bool is_sym(int cfg) { return cfg >= nb::NB_PAIR_CONFIGS; }
+}  // namespace
 
 struct nb_batch {
     int device = 0;
@@ -25,6 +35,12 @@ struct nb_batch {
     float* part = nullptr;
     size_t part_floats = 0;
     nbpair::Plan plan{};
+    // symmetric kernel: per-system table, padded FP32 records, i-side and j-side partials
+    nbsym::SymSys* sym_table = nullptr;
+    float4* sym_src = nullptr;
+    float* sym_part_i = nullptr;
+    float* sym_part_j = nullptr;
+    nbsym::SymPlan sym_plan{};
 };
 
 
@@ -58,6 +74,21 @@ nb_status host_plan(const nb_batch* b, int cfg, int sm_count, HostPlan* hp) {
 }
 
 nb_status apply_config(nb_batch* b, int cfg, int sm_count) {
+    if (is_sym(cfg)) {
+        nb::SymHostPlan sp;
+        NB_TRY(nb::sym_host_plan(cfg - nb::NB_PAIR_CONFIGS, b->counts.data(), b->n_systems,
+                                 sm_count, &sp));
+        NB_CUDA_TRY(cudaMemcpy(b->sym_table, sp.sys.data(), sp.sys.size() * sizeof(nbsym::SymSys),
+                               cudaMemcpyHostToDevice));
+        b->sym_plan.sys = b->sym_table;
+        b->sym_plan.n_systems = b->n_systems;
+        b->sym_plan.ctas = sp.ctas;
+        b->sym_plan.n_total = sp.n_total;
+        b->sym_plan.n_records = sp.n_records;
+        b->sym_plan.units = sp.units;
+        b->cfg = cfg;
+        return NB_OK;
+    }
     HostPlan hp;
     NB_TRY(host_plan(b, cfg, sm_count, &hp));
     NB_CUDA_TRY(cudaMemcpy(b->unit_off, hp.unit_off.data(), hp.unit_off.size() * 8,
@@ -72,6 +103,10 @@ nb_status apply_config(nb_batch* b, int cfg, int sm_count) {
 nb_status batch_accel(nb_ctx* ctx, nb_batch* b, const double* m, const double* x, const double* y,
                       const double* z, double* ax, double* ay, double* az, double G, double eps2,
                       cudaStream_t s) {
+    if (is_sym(b->cfg))
+        return nb::sym_launch(b->cfg - nb::NB_PAIR_CONFIGS, b->sym_plan, m, x, y, z, G, eps2,
+                              b->sym_src, b->sym_part_i, b->sym_part_j, ax, ay, az,
+                              ctx->dev_error, s);
     if (b->plan.units == 0) return NB_OK;
     return nb::pair_launch(b->cfg, b->plan, m, x, y, z, b->n_total, b->n_total, G, eps2, b->src,
                            b->tgt, b->part, ax, ay, az, ctx->dev_error, s);
@@ -114,11 +149,26 @@ nb_status nb_batch_create(nb_ctx* ctx, uint32_t n_systems, const uint32_t* count
         if (f > part_floats) part_floats = f;
     }
     b->part_floats = part_floats;
+    // symmetric configurations: the largest records and partials of any of them
+    size_t sym_records = 0, sym_pi = 0, sym_pj = 0;
+    for (int c = 0; c < nb::NB_SYM_CONFIGS; ++c) {
+        nb::SymHostPlan sp;
+        nb_status st = nb::sym_host_plan(c, b->counts.data(), n_systems, ctx->sm_count, &sp);
+        if (st != NB_OK) {
+            delete b;
+            return st;
+        }
+        sym_records = std::max(sym_records, (size_t)sp.n_records);
+        sym_pi = std::max(sym_pi, nb::sym_part_i_floats(c, sp.ctas, sp.n_blocks));
+        sym_pj = std::max(sym_pj, nb::sym_part_j_floats(c, sp.units));
+    }
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t ns = n_systems + 1;
     const size_t sizes[] = {al(ns * 4), al(ns * 4), al(ns * 4), al(ns * 4), al(ns * 8),
                             al((size_t)b->n_total * sizeof(nbpair::SrcDup) + 32),
-                            al((size_t)b->n_total * sizeof(float4) + 16), al(part_floats * 4)};
+                            al((size_t)b->n_total * sizeof(float4) + 16), al(part_floats * 4),
+                            al(ns * sizeof(nbsym::SymSys)), al(sym_records * sizeof(float4)),
+                            al(sym_pi * 4), al(sym_pj * 4)};
     size_t total = 0;
     for (size_t v : sizes) total += v;
     cudaError_t e = cudaMalloc(&b->mem, total);
@@ -134,7 +184,11 @@ nb_status nb_batch_create(nb_ctx* ctx, uint32_t n_systems, const uint32_t* count
     b->unit_off = (uint64_t*)p; p += sizes[4];
     b->src = (nbpair::SrcDup*)p; p += sizes[5];
     b->tgt = (float4*)p; p += sizes[6];
-    b->part = (float*)p;
+    b->part = (float*)p; p += sizes[7];
+    b->sym_table = (nbsym::SymSys*)p; p += sizes[8];
+    b->sym_src = (float4*)p; p += sizes[9];
+    b->sym_part_i = (float*)p; p += sizes[10];
+    b->sym_part_j = (float*)p;
     std::vector<uint32_t> zeros(n_systems, 0);
     e = cudaMemcpy(b->sys_off, off.data(), ns * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->t_off, off.data(), ns * 4, cudaMemcpyHostToDevice);
@@ -170,18 +224,29 @@ nb_status nb_batch_destroy(nb_batch* b) {
 nb_status nb_batch_info(const nb_batch* b, uint32_t* n_total, int* config, int* threads,
                         int* targets_per_thread, int* j_tile) {
     if (!b) return nb::set_error(NB_ERR_INVALID_ARG, "nb_batch_info: null batch");
-    const nb::PairConfig& C = nb::kPairConfigs[b->cfg];
+    int t = 0, ip = 0, jt = 0;
+    if (is_sym(b->cfg)) {
+        const nb::SymConfig& C = nb::kSymConfigs[b->cfg - nb::NB_PAIR_CONFIGS];
+        t = 32 * C.warps;
+        ip = C.p;
+        jt = C.jt;
+    } else {
+        const nb::PairConfig& C = nb::kPairConfigs[b->cfg];
+        t = C.threads;
+        ip = C.ip;
+        jt = C.jt;
+    }
     if (n_total) *n_total = b->n_total;
     if (config) *config = b->cfg;
-    if (threads) *threads = C.threads;
-    if (targets_per_thread) *targets_per_thread = C.ip;
-    if (j_tile) *j_tile = C.jt;
+    if (threads) *threads = t;
+    if (targets_per_thread) *targets_per_thread = ip;
+    if (j_tile) *j_tile = jt;
     return NB_OK;
 }
 
 nb_status nb_batch_set_config(nb_ctx* ctx, nb_batch* b, int config) {
     NB_CHECK_CTX(ctx);
-    if (!b || config < 0 || config >= nb::NB_PAIR_CONFIGS)
+    if (!b || config < 0 || config >= NB_BATCH_CONFIGS)
         return nb::set_error(NB_ERR_INVALID_ARG, "nb_batch_set_config: bad arguments");
     return apply_config(b, config, ctx->sm_count);
 }
@@ -206,7 +271,7 @@ nb_status nb_batch_autotune(nb_ctx* ctx, nb_batch* b, const double* m, const dou
     int best = 0;
     float best_ms = 0;
     nb_status st = NB_OK;
-    for (int c = 0; c < nb::NB_PAIR_CONFIGS && st == NB_OK; ++c) {
+    for (int c = 0; c < NB_BATCH_CONFIGS && st == NB_OK; ++c) {
         st = apply_config(b, c, ctx->sm_count);
         if (st != NB_OK) break;
         st = batch_accel(ctx, b, m, x, y, z, ax, ay, az, G, eps2, nullptr);  // warm-up

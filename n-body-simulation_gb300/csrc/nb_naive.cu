@@ -193,15 +193,28 @@ int g_naive_sym_cfg = 0;
 constexpr uint64_t SYM_MIN_UNITS_PER_CTA = 8;
 constexpr size_t SYM_PART_CAP_BYTES = (size_t)4 << 30;
 
-nb_status naive_f32c_sym(nb_ctx* ctx, int cfg, const nbsym::SymPlan& S, const double* m,
+nb_status naive_f32c_sym(nb_ctx* ctx, int cfg, const nb::SymHostPlan& hp, const double* m,
                          const double* x, const double* y, const double* z, double* ax,
                          double* ay, double* az, double G, double eps2, cudaStream_t stream) {
-    const size_t src_bytes = (nb::sym_src_bytes(cfg, S) + 255) & ~(size_t)255;
-    const size_t pi_bytes = (nb::sym_part_i_floats(cfg, S) * sizeof(float) + 255) & ~(size_t)255;
-    const size_t pj_bytes = nb::sym_part_j_floats(cfg, S) * sizeof(float);
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t table_bytes = al(2 * sizeof(nbsym::SymSys));
+    const size_t src_bytes = al((size_t)hp.n_records * sizeof(float4));
+    const size_t pi_bytes = al(nb::sym_part_i_floats(cfg, hp.ctas, hp.n_blocks) * sizeof(float));
+    const size_t pj_bytes = nb::sym_part_j_floats(cfg, hp.units) * sizeof(float);
     void* base = nullptr;
-    NB_TRY(nb::scratch(ctx, NB_SCRATCH_PAIR_SYM, src_bytes + pi_bytes + pj_bytes, &base));
+    NB_TRY(nb::scratch(ctx, NB_SCRATCH_PAIR_SYM, table_bytes + src_bytes + pi_bytes + pj_bytes,
+                       &base));
     char* b = (char*)base;
+    nbsym::SymSys* table = (nbsym::SymSys*)b;
+    NB_TRY(nb::sym_single_table(table, hp, stream));
+    nbsym::SymPlan S;
+    S.sys = table;
+    S.n_systems = 1;
+    S.ctas = hp.ctas;
+    S.n_total = hp.n_total;
+    S.n_records = hp.n_records;
+    S.units = hp.units;
+    b += table_bytes;
     return nb::sym_launch(cfg, S, m, x, y, z, G, eps2, (float4*)b, (float*)(b + src_bytes),
                           (float*)(b + src_bytes + pi_bytes), ax, ay, az, ctx->dev_error, stream);
 }
@@ -212,14 +225,13 @@ nb_status naive_f32c(nb_ctx* ctx, const double* m, const double* x, const double
                      cudaStream_t stream) {
     if (i_begin == 0 && i_end == n && g_naive_sym_mode != 0) {
         const int scfg = g_naive_sym_cfg;
-        int sym_per_sm = 0;
-        NB_TRY(nb::sym_ctas_per_sm(scfg, &sym_per_sm));
-        const nbsym::SymPlan S = nb::sym_plan(scfg, n, (uint32_t)(ctx->sm_count * sym_per_sm));
+        nb::SymHostPlan hp;
+        NB_TRY(nb::sym_host_plan(scfg, &n, 1, ctx->sm_count, &hp));
         const bool use =
             g_naive_sym_mode == 2 ||
-            (S.units >= SYM_MIN_UNITS_PER_CTA * S.ctas &&
-             nb::sym_part_j_floats(scfg, S) * sizeof(float) <= SYM_PART_CAP_BYTES);
-        if (use) return naive_f32c_sym(ctx, scfg, S, m, x, y, z, ax, ay, az, G, eps2, stream);
+            (hp.units >= SYM_MIN_UNITS_PER_CTA * hp.ctas &&
+             nb::sym_part_j_floats(scfg, hp.units) * sizeof(float) <= SYM_PART_CAP_BYTES);
+        if (use) return naive_f32c_sym(ctx, scfg, hp, m, x, y, z, ax, ay, az, G, eps2, stream);
     }
     const int cfg = g_naive_pair_cfg;
     const nb::PairConfig& C = nb::kPairConfigs[cfg];

@@ -35,40 +35,78 @@ using nbpair::mbar_expect_tx;
 using nbpair::mbar_init;
 using nbpair::mbar_wait;
 
-// Largest a in [0, nb) with unit_off(a) <= u.
-__device__ __forceinline__ uint32_t locate(const SymPlan& S, uint64_t u) {
-    uint32_t lo = 0, hi = S.nb;
+// Largest s in [0, count) with key(s) <= v (key non-decreasing in s, key(0) <= v).
+template <typename F, typename T>
+__device__ __forceinline__ uint32_t last_le(uint32_t count, T v, F key) {
+    uint32_t lo = 0, hi = count;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (unit_off(S, mid) <= u) lo = mid; else hi = mid;
+        if (key(mid) <= v) lo = mid; else hi = mid;
     }
     return lo;
 }
 
-__device__ __forceinline__ uint64_t unit_begin(const SymPlan& S, uint32_t cta) {
-    return (S.units * (uint64_t)cta) / S.ctas;
+__device__ __forceinline__ uint64_t unit_begin(const SymPlan& P, uint32_t cta) {
+    return (P.units * (uint64_t)cta) / P.ctas;
 }
 
-__device__ __forceinline__ uint32_t cta_of_unit(const SymPlan& S, uint64_t u) {
-    uint32_t c = (uint32_t)((u * S.ctas) / S.units);
-    while (c + 1 < S.ctas && unit_begin(S, c + 1) <= u) ++c;
-    while (c > 0 && unit_begin(S, c) > u) --c;
+__device__ __forceinline__ uint32_t cta_of_unit(const SymPlan& P, uint64_t u) {
+    uint32_t c = (uint32_t)((u * P.ctas) / P.units);
+    while (c + 1 < P.ctas && unit_begin(P, c + 1) <= u) ++c;
+    while (c > 0 && unit_begin(P, c) > u) --c;
     return c;
 }
 
-// Positions relative to body 0 (FP64 subtraction, then rounded) and G*m in FP32; bodies beyond n
-// up to the padded count are massless and far away (they add exactly 0 to every real body).
-__global__ void sym_prepare_kernel(const double* __restrict__ m, const double* __restrict__ x,
-                                   const double* __restrict__ y, const double* __restrict__ z,
-                                   uint32_t n, uint32_t n_pad, double G,
+// Where a unit lies: system s (its bodies, I-blocks, j-tiles, records and first unit and
+// I-block), I-block a and j-tile jt inside it.
+struct Loc {
+    uint32_t s, nb, n_jt, poff, bbase, a, jt;
+    uint64_t ubase;
+};
+
+template <uint32_t TPB, int JT>
+__device__ __forceinline__ Loc locate(const SymPlan& P, uint64_t u) {
+    Loc L;
+    L.s = last_le(P.n_systems, u, [&](uint32_t k) { return P.sys[k].uoff; });
+    const SymSys A = P.sys[L.s], B = P.sys[L.s + 1];
+    L.nb = B.boff - A.boff;
+    L.n_jt = (B.off - A.off + JT - 1) / JT;
+    L.poff = A.poff;
+    L.bbase = A.boff;
+    L.ubase = A.uoff;
+    const uint64_t lu = u - A.uoff;
+    L.a = last_le(L.nb, lu, [&](uint32_t k) { return row_off(L.n_jt, TPB, k); });
+    L.jt = L.a * TPB + (uint32_t)(lu - row_off(L.n_jt, TPB, L.a));
+    return L;
+}
+
+// FP32 records of all systems, each padded to whole I-blocks: positions relative to the
+// system's first body (FP64 subtraction, then rounded) and G*m; pad records are massless and
+// far away (they add exactly 0 to every real body).
+__global__ void sym_prepare_kernel(SymPlan P, const double* __restrict__ m,
+                                   const double* __restrict__ x, const double* __restrict__ y,
+                                   const double* __restrict__ z, double G,
                                    float4* __restrict__ out) {
-    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= n_pad) return;
-    if (b < n)
-        out[b] = make_float4((float)(x[b] - x[0]), (float)(y[b] - y[0]), (float)(z[b] - z[0]),
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P.n_records) return;
+    const uint32_t s = last_le(P.n_systems, r, [&](uint32_t k) { return P.sys[k].poff; });
+    const SymSys A = P.sys[s], B = P.sys[s + 1];
+    const uint32_t t = r - A.poff;
+    if (t < B.off - A.off) {
+        const uint32_t b = A.off + t, a0 = A.off;
+        out[r] = make_float4((float)(x[b] - x[a0]), (float)(y[b] - y[a0]), (float)(z[b] - z[a0]),
                              (float)(G * m[b]));
-    else
-        out[b] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+    } else {
+        out[r] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+    }
+}
+
+// The table of a single system of n bodies (nb I-blocks, `records` padded records, `units`
+// units), written by a kernel so that it can be part of a captured graph.
+__global__ void sym_single_table_kernel(SymSys* sys, uint32_t n, uint32_t nb, uint32_t records,
+                                        uint64_t units) {
+    sys[0] = SymSys{0, 0, 0, 0, 0};
+    sys[1] = SymSys{units, n, records, nb, 0};
 }
 
 template <int W, int P, int JT>
@@ -98,20 +136,16 @@ pair_sym_kernel(SymPlan S, const float4* __restrict__ src, float eps2, float* __
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    // Thread 0's copy cursor: the I-block and j-tile of the next unit to copy.
-    uint32_t c_a = 0, c_jt = 0;
+    // Thread 0 copies the j-tile of unit c_u into buffer buf and moves on to the next unit.
+    uint64_t c_u = u0;
     auto issue = [&](int buf) {
+        const Loc L = locate<TPB, JT>(S, c_u);
         mbar_expect_tx(&full[buf], JT * (uint32_t)sizeof(float4));
-        bulk_g2s(&tile[buf][0], src + (size_t)c_jt * JT, JT * (uint32_t)sizeof(float4),
+        bulk_g2s(&tile[buf][0], src + L.poff + (size_t)L.jt * JT, JT * (uint32_t)sizeof(float4),
                  &full[buf]);
-        if (++c_jt == S.n_jt) {
-            ++c_a;
-            c_jt = c_a * TPB;
-        }
+        ++c_u;
     };
     if (threadIdx.x == 0) {
-        c_a = locate(S, u0);
-        c_jt = c_a * TPB + (uint32_t)(u0 - unit_off(S, c_a));
         issue(0);
         if (u0 + 1 < u1) issue(1);
     }
@@ -122,10 +156,11 @@ pair_sym_kernel(SymPlan S, const float4* __restrict__ src, float eps2, float* __
     uint32_t iter = 0;
     bool failed = false;
     while (u < u1 && !failed) {
-        const uint32_t a = locate(S, u);
-        const uint64_t seg_end = min(u1, unit_off(S, a + 1));
-        uint32_t jt = a * TPB + (uint32_t)(u - unit_off(S, a));
-        const float4* isrc = src + (size_t)a * IB + w * 32 * P + lane;
+        const Loc L = locate<TPB, JT>(S, u);
+        const uint32_t a = L.a;
+        const uint64_t seg_end = min(u1, L.ubase + row_off(L.n_jt, TPB, a + 1));
+        uint32_t jt = L.jt;
+        const float4* isrc = src + L.poff + (size_t)a * IB + w * 32 * P + lane;
 #pragma unroll
         for (int k = 0; k < P; ++k) {
             const float4 b = isrc[k * 32];
@@ -206,7 +241,7 @@ pair_sym_kernel(SymPlan S, const float4* __restrict__ src, float eps2, float* __
             if (threadIdx.x == 0 && u + 2 < u1) issue(buf);  // the cursor is at u + 2
         }
         if (failed) break;
-        float* out = part_i + (size_t)(cta + a) * 6 * IB + w * 32 * P + lane;
+        float* out = part_i + (size_t)(cta + L.bbase + a) * 6 * IB + w * 32 * P + lane;
 #pragma unroll
         for (int k = 0; k < P; ++k)
 #pragma unroll
@@ -226,26 +261,31 @@ __global__ void sym_combine_kernel(SymPlan S, const float* __restrict__ part_i,
                                    const float* __restrict__ part_j, double* __restrict__ ax,
                                    double* __restrict__ ay, double* __restrict__ az) {
     constexpr uint32_t TPB = IB / JT;
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= S.n) return;
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= S.n_total) return;
+    const uint32_t s = last_le(S.n_systems, b, [&](uint32_t k) { return S.sys[k].off; });
+    const SymSys A = S.sys[s], B = S.sys[s + 1];
+    const uint32_t n_jt = (B.off - A.off + JT - 1) / JT;
+    const uint32_t t = b - A.off;
     const uint32_t a = t / IB, li = t % IB, jt = t / JT, jl = t % JT;
-    const uint32_t c0 = cta_of_unit(S, unit_off(S, a)), c1 = cta_of_unit(S, unit_off(S, a + 1) - 1);
+    const uint32_t c0 = cta_of_unit(S, A.uoff + row_off(n_jt, TPB, a));
+    const uint32_t c1 = cta_of_unit(S, A.uoff + row_off(n_jt, TPB, a + 1) - 1);
     double sx = 0, sy = 0, sz = 0;
     for (uint32_t c = c0; c <= c1; ++c) {
-        const float* p = part_i + (size_t)(c + a) * 6 * IB;
+        const float* p = part_i + (size_t)(c + A.boff + a) * 6 * IB;
         sx += (double)p[0 * IB + li] + (double)p[3 * IB + li];
         sy += (double)p[1 * IB + li] + (double)p[4 * IB + li];
         sz += (double)p[2 * IB + li] + (double)p[5 * IB + li];
     }
-    for (uint32_t b = 0; b < a; ++b) {
-        const float* p = part_j + (unit_off(S, b) + (jt - b * TPB)) * 3 * JT;
+    for (uint32_t r = 0; r < a; ++r) {
+        const float* p = part_j + (A.uoff + row_off(n_jt, TPB, r) + (jt - r * TPB)) * 3 * JT;
         sx += (double)p[jl];
         sy += (double)p[JT + jl];
         sz += (double)p[2 * JT + jl];
     }
-    ax[t] = sx;
-    ay[t] = sy;
-    az[t] = sz;
+    ax[b] = sx;
+    ay[b] = sy;
+    az[b] = sz;
 }
 
 }  // namespace nbsym
@@ -292,7 +332,7 @@ nb_status sym_launch_cfg(const nbsym::SymPlan& S, const float4* src, float eps2,
     nbsym::pair_sym_kernel<W, P, JT><<<S.ctas, 32 * W, sym_smem_bytes<W, P, JT>(), stream>>>(
         S, src, eps2, part_i, part_j, err_word);
     NB_TRY(check_launch("pair_sym_kernel"));
-    nbsym::sym_combine_kernel<32 * W * P, JT><<<ceil_div(S.n, 256), 256, 0, stream>>>(
+    nbsym::sym_combine_kernel<32 * W * P, JT><<<ceil_div(S.n_total, 256), 256, 0, stream>>>(
         S, part_i, part_j, ax, ay, az);
     return check_launch("sym_combine_kernel");
 }
@@ -316,27 +356,45 @@ nb_status sym_ctas_per_sm(int cfg, int* out) {
     return NB_OK;
 }
 
-nbsym::SymPlan sym_plan(int cfg, uint32_t n, uint32_t ctas_max) {
+nb_status sym_host_plan(int cfg, const uint32_t* counts, uint32_t n_systems, int sm_count,
+                        SymHostPlan* out) {
     const SymConfig& C = kSymConfigs[cfg];
-    const uint32_t ib = 32u * C.warps * C.p;
-    nbsym::SymPlan S;
-    S.n = n;
-    S.nb = (n + ib - 1) / ib;
-    S.tpb = ib / C.jt;
-    S.n_jt = S.nb * S.tpb;
-    S.units = nbsym::unit_off(S, S.nb);
-    S.ctas = (uint32_t)(S.units < ctas_max ? S.units : ctas_max);
-    return S;
+    const uint32_t ib = sym_ib(cfg), tpb = ib / (uint32_t)C.jt;
+    out->sys.assign(n_systems + 1, nbsym::SymSys{0, 0, 0, 0, 0});
+    for (uint32_t s = 0; s < n_systems; ++s) {
+        const nbsym::SymSys& A = out->sys[s];
+        const uint32_t n = counts[s];
+        const uint32_t nb = (n + ib - 1) / ib, n_jt = (n + C.jt - 1) / C.jt;
+        const uint64_t records = (uint64_t)A.poff + (uint64_t)nb * ib;
+        if (records > 0xffffffffull)
+            return set_error(NB_ERR_INVALID_ARG, "symmetric pair plan: more than 2^32 records");
+        out->sys[s + 1] = nbsym::SymSys{A.uoff + nbsym::row_off(n_jt, tpb, nb), A.off + n,
+                                        (uint32_t)records, A.boff + nb, 0};
+    }
+    int per_sm = 0;
+    NB_TRY(sym_ctas_per_sm(cfg, &per_sm));
+    const nbsym::SymSys& E = out->sys[n_systems];
+    out->units = E.uoff;
+    out->n_total = E.off;
+    out->n_records = E.poff;
+    out->n_blocks = E.boff;
+    uint64_t ctas = (uint64_t)sm_count * per_sm;
+    if (ctas > out->units) ctas = out->units;
+    out->ctas = (uint32_t)(ctas ? ctas : 1);
+    return NB_OK;
 }
 
-size_t sym_src_bytes(int cfg, const nbsym::SymPlan& S) {
-    return (size_t)S.n_jt * kSymConfigs[cfg].jt * sizeof(float4);
+size_t sym_part_i_floats(int cfg, uint32_t ctas, uint32_t n_blocks) {
+    return ((size_t)ctas + n_blocks) * 6 * sym_ib(cfg);
 }
-size_t sym_part_i_floats(int cfg, const nbsym::SymPlan& S) {
-    return ((size_t)S.ctas + S.nb) * 6 * 32 * kSymConfigs[cfg].warps * kSymConfigs[cfg].p;
+size_t sym_part_j_floats(int cfg, uint64_t units) {
+    return (size_t)units * 3 * kSymConfigs[cfg].jt;
 }
-size_t sym_part_j_floats(int cfg, const nbsym::SymPlan& S) {
-    return (size_t)S.units * 3 * kSymConfigs[cfg].jt;
+
+nb_status sym_single_table(nbsym::SymSys* sys, const SymHostPlan& hp, cudaStream_t stream) {
+    const nbsym::SymSys& E = hp.sys[1];
+    nbsym::sym_single_table_kernel<<<1, 1, 0, stream>>>(sys, E.off, E.boff, E.poff, E.uoff);
+    return check_launch("sym_single_table_kernel");
 }
 
 nb_status sym_launch(int cfg, const nbsym::SymPlan& S, const double* m, const double* x,
@@ -345,14 +403,15 @@ nb_status sym_launch(int cfg, const nbsym::SymPlan& S, const double* m, const do
                      uint32_t* err_word, cudaStream_t stream) {
     int per_sm = 0;
     NB_TRY(sym_ctas_per_sm(cfg, &per_sm));  // shared-memory opt-in before the first launch
-    const uint32_t n_pad = S.n_jt * (uint32_t)kSymConfigs[cfg].jt;
-    nbsym::sym_prepare_kernel<<<ceil_div(n_pad, 256), 256, 0, stream>>>(m, x, y, z, S.n, n_pad, G,
-                                                                        src);
+    if (S.units == 0) return NB_OK;
+    nbsym::sym_prepare_kernel<<<ceil_div(S.n_records, 256), 256, 0, stream>>>(S, m, x, y, z, G,
+                                                                              src);
     NB_TRY(check_launch("sym_prepare_kernel"));
     switch (cfg) {
-#define NB_SYM_LAUNCH(i, W, P, JT) \
-    case i:                        \
-        return sym_launch_cfg<W, P, JT>(S, src, (float)eps2, part_i, part_j, ax, ay, az, err_word, stream);
+#define NB_SYM_LAUNCH(i, W, P, JT)                                                               \
+    case i:                                                                                      \
+        return sym_launch_cfg<W, P, JT>(S, src, (float)eps2, part_i, part_j, ax, ay, az, err_word, \
+                                        stream);
         NB_SYM_CONFIG_LIST(NB_SYM_LAUNCH)
 #undef NB_SYM_LAUNCH
         default: return set_error(NB_ERR_INVALID_ARG, "bad symmetric pair config %d", cfg);

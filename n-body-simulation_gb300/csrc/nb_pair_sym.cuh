@@ -1,20 +1,31 @@
 // nb_pair_sym.cuh -- plan and launcher of the symmetric FP32 pair kernel (nb_pair_sym.cu).
 #pragma once
+#include <vector>
+
 #include "nb_internal.cuh"
 
 namespace nbsym {
 
-// One system of n bodies in nb I-blocks of IB bodies and n_jt = nb * tpb j-tiles of JT bodies;
-// row a of the unit sequence holds the j-tiles a * tpb .. n_jt - 1.
+// One entry per system plus a closing entry with the totals (prefix sums): first unit, first
+// body in the FP64 arrays, first padded FP32 record and first I-block of system s. System s has
+// off[s+1] - off[s] bodies in boff[s+1] - boff[s] I-blocks of IB bodies (records padded to whole
+// I-blocks) and ceil(n / JT) j-tiles of JT bodies.
+struct SymSys {
+    uint64_t uoff;
+    uint32_t off, poff, boff, pad;
+};
+
 struct SymPlan {
-    uint32_t n, nb, n_jt, tpb, ctas;
+    const SymSys* sys;  // device, n_systems + 1 entries
+    uint32_t n_systems, ctas, n_total, n_records;
     uint64_t units;
 };
 
-// First unit of I-block a (a <= nb; unit_off(nb) = units).
-__host__ __device__ __forceinline__ uint64_t unit_off(const SymPlan& S, uint32_t a) {
+// First unit of I-block a of a system with n_jt j-tiles (row a holds the j-tiles a * tpb ..
+// n_jt - 1; a = nb gives the system's unit count).
+__host__ __device__ __forceinline__ uint64_t row_off(uint32_t n_jt, uint32_t tpb, uint32_t a) {
     const uint64_t aa = a;
-    return aa * S.n_jt - (uint64_t)S.tpb * (aa == 0 ? 0 : aa * (aa - 1) / 2);
+    return aa * n_jt - (uint64_t)tpb * (aa == 0 ? 0 : aa * (aa - 1) / 2);
 }
 
 }  // namespace nbsym
@@ -27,15 +38,26 @@ struct SymConfig {
 constexpr int NB_SYM_CONFIGS = 8;
 extern const SymConfig kSymConfigs[NB_SYM_CONFIGS];
 
+// Bodies per I-block of configuration cfg.
+inline uint32_t sym_ib(int cfg) { return 32u * kSymConfigs[cfg].warps * kSymConfigs[cfg].p; }
+
 // Resident CTAs per SM of configuration cfg (also opts it into its dynamic shared memory).
 nb_status sym_ctas_per_sm(int cfg, int* out);
-// Plan of one system of n bodies with at most ctas_max persistent CTAs.
-nbsym::SymPlan sym_plan(int cfg, uint32_t n, uint32_t ctas_max);
-// Scratch sizes of a plan: padded FP32 sources (bytes) and the two partial buffers (floats).
-size_t sym_src_bytes(int cfg, const nbsym::SymPlan& S);
-size_t sym_part_i_floats(int cfg, const nbsym::SymPlan& S);
-size_t sym_part_j_floats(int cfg, const nbsym::SymPlan& S);
-// Launches prepare + symmetric pair kernel + combine.
+
+// Host side of a plan: the per-system table and the totals.
+struct SymHostPlan {
+    std::vector<nbsym::SymSys> sys;
+    uint64_t units = 0;
+    uint32_t n_total = 0, n_records = 0, n_blocks = 0, ctas = 0;
+};
+nb_status sym_host_plan(int cfg, const uint32_t* counts, uint32_t n_systems, int sm_count,
+                        SymHostPlan* out);
+// Scratch of a plan: FP32 records (n_records float4), i-side and j-side partials (floats).
+size_t sym_part_i_floats(int cfg, uint32_t ctas, uint32_t n_blocks);
+size_t sym_part_j_floats(int cfg, uint64_t units);
+// Writes the device table of a single-system plan (two entries) with a kernel.
+nb_status sym_single_table(nbsym::SymSys* sys, const SymHostPlan& hp, cudaStream_t stream);
+// Launches prepare + symmetric pair kernel + combine for a plan whose device table is filled.
 nb_status sym_launch(int cfg, const nbsym::SymPlan& S, const double* m, const double* x,
                      const double* y, const double* z, double G, double eps2, float4* src,
                      float* part_i, float* part_j, double* ax, double* ay, double* az,

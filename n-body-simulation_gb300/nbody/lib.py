@@ -455,7 +455,7 @@ class Batch:
                                             stream_ptr(stream)))
 
     def autotune(self, m, x, y, z, ax, ay, az, G, eps2, reps=3):
-        ms = (C.c_float * PAIR_CONFIGS)()
+        ms = (C.c_float * BATCH_CONFIGS)()
         chosen = _i()
         check(self.lib.nb_batch_autotune(self.ctx.handle, self.handle, ptr(m), ptr(x), ptr(y),
                                          ptr(z), ptr(ax), ptr(ay), ptr(az), G, eps2, reps, ms,
@@ -492,6 +492,7 @@ class Graph:
 
 MLP_PARAMS = 1377
 PAIR_CONFIGS = 8  # NB_PAIR_CONFIG_COUNT
+BATCH_CONFIGS = 16  # NB_BATCH_CONFIG_COUNT: the one-sided shapes, then the symmetric ones
 
 
 def mlp_loss_grad(ctx, params, X, Y, idx, n, grad, loss, stream=None):

@@ -49,11 +49,14 @@ def run_batch(ctx, b, cat, eps2=1e-6):
 COUNTS = [1, 2, 3, 0, 300, 1023, 1024, 1025, 2500, 7000, 5]
 
 
-def test_batch_matches_oracle_per_system(ctx):
+@pytest.mark.parametrize("config", [0, 8])
+def test_batch_matches_oracle_per_system(ctx, config):
+    """Configuration 0: the one-sided kernel; 8: the symmetric kernel's default shape."""
     from nbody.lib import Batch
     cat = ensemble(COUNTS)
     b = Batch(ctx, COUNTS)
     assert b.info()["n_total"] == sum(COUNTS)
+    b.set_config(config)
     got = run_batch(ctx, b, cat)
     off = 0
     for n in COUNTS:
@@ -69,9 +72,12 @@ def test_batch_matches_oracle_per_system(ctx):
         off += n
 
 
-@pytest.mark.parametrize("config", range(8))
+@pytest.mark.parametrize("config", range(16))
 def test_every_configuration(ctx, config):
-    from nbody.lib import Batch, set_naive_pair_config
+    """Every shape of both kernels (0-7 one-sided, 8-15 symmetric) against configuration 0, and
+    the single-system entry point with the same shape against the oracle."""
+    from nbody.lib import (PAIR_CONFIGS, SYM_ALWAYS, SYM_AUTO, Batch, set_naive_pair_config,
+                           set_naive_symmetric)
     cat = ensemble(COUNTS, seed=3)
     b = Batch(ctx, COUNTS)
     b.set_config(config)
@@ -89,11 +95,15 @@ def test_every_configuration(ctx, config):
     t = {k: dev(d[k]) for k in ("m", "x", "y", "z")}
     a = [torch.zeros(5000, dtype=torch.float64, device="cuda") for _ in range(3)]
     try:
-        set_naive_pair_config(config)
+        if config < PAIR_CONFIGS:
+            set_naive_pair_config(config)
+        else:
+            set_naive_symmetric(SYM_ALWAYS, config - PAIR_CONFIGS)
         ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, 1.0, 1e-6, "f32c")
         ctx.sync()
     finally:
         set_naive_pair_config(0)
+        set_naive_symmetric(SYM_AUTO, 0)
     err = rel_err(*[host(v) for v in a], *oracle.naive_accel(d["m"], d["x"], d["y"], d["z"], 1.0, 1e-6))
     assert np.median(err) <= 1e-5 and err.max() <= 1e-3
 
@@ -107,18 +117,20 @@ def test_autotune_picks_a_configuration(ctx):
     t = {k: dev(cat[k]) for k in ("m", "x", "y", "z")}
     a = [torch.zeros(len(cat["m"]), dtype=torch.float64, device="cuda") for _ in range(3)]
     chosen, ms = b.autotune(t["m"], t["x"], t["y"], t["z"], *a, 1.0, 1e-6, reps=2)
-    assert 0 <= chosen < 6 and all(v > 0 for v in ms)
+    assert 0 <= chosen < 16 and len(ms) == 16 and all(v > 0 for v in ms)
     assert ms[chosen] == min(ms)
     assert b.info()["config"] == chosen
 
 
-def test_graph_replay_equals_stepwise_calls(ctx):
+@pytest.mark.parametrize("config", [0, 8])
+def test_graph_replay_equals_stepwise_calls(ctx, config):
     import torch
     from nbody.lib import Batch
     counts = [500, 1200, 77, 3000]
     cat = ensemble(counts, seed=11)
     n = len(cat["m"])
     b = Batch(ctx, counts)
+    b.set_config(config)
 
     def state():
         s = {k: dev(cat[k]) for k in ("m", "x", "y", "z", "vx", "vy", "vz")}
