@@ -439,7 +439,7 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
     import torch
 
     from nbody import generators, workloads
-    from nbody.lib import fma_peak
+    from nbody.lib import SYM_AUTO, SYM_NEVER, fma_peak, set_naive_symmetric
 
     out = {}
 
@@ -501,9 +501,21 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
     a = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(3)]
     ms = timed(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, dd["G"], EPS2, "f64"), 5)
     gp = n * n / (ms * 1e-3) / 1e9
-    out["naive_f64_disc_16384"] = {"ms_per_eval": ms, "gpairs_per_s": gp,
-                                   "frac_of_measured_fp64_fma_peak":
-                                       gp * 20e9 / fma_peak(ctx, fp64=True)}
+    set_naive_symmetric(SYM_NEVER)
+    ms1 = timed(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, dd["G"], EPS2, "f64"),
+                3)
+    set_naive_symmetric(SYM_AUTO)
+    gp1 = n * n / (ms1 * 1e-3) / 1e9
+    peak64 = fma_peak(ctx, fp64=True)
+    out["naive_f64_disc_16384"] = {
+        "kernel": "pair_sym_kernel<double> (each unordered pair once, added to both bodies: 20 "
+                  "FP64 operations per unordered pair = 10 per ordered pair)",
+        "ms_per_eval": ms, "gpairs_per_s": gp,
+        "frac_of_measured_fp64_fma_peak": gp * 20e9 / peak64,
+        "executed_fp64_ops_frac_of_measured_peak": gp * 10e9 / (peak64 / 2),
+        "one_sided": {"kernel": "naive_f64_kernel (16 FP64 operations per ordered pair)",
+                      "ms_per_eval": ms1, "gpairs_per_s": gp1,
+                      "frac_of_measured_fp64_fma_peak": gp1 * 20e9 / peak64}}
     ms = timed(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, dd["G"], EPS2, "df64"),
                5)
     out["naive_df64_disc_16384"] = {

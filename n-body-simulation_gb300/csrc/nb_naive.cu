@@ -5,8 +5,10 @@
 //    operation separately rounded in the reference's order (r^2 summed left to right, den^3 as
 //    (den*den)*den, 1/sqrt for rsqrt, acc += m*(r*den), G last). Bit-identical to the host
 //    FP64 evaluation of NaiveAlgorithm.cpp:331-351.
-//  * NB_F64: same loop with FMAs and m (r^2 + eps^2)^(-3/2) from the hardware rsqrt estimate with
-//    one correction (nb_m_rinv3_f64; FP64-pipe bound on GB300).
+//  * NB_F64: over all bodies of a large system, the FP64 form of the symmetric pair kernel of
+//    nb_pair_sym.cu (each unordered pair once, 20 FP64 operations for both bodies); otherwise the
+//    same loop as the IEEE mode with FMAs and m (r^2 + eps^2)^(-3/2) from the hardware rsqrt
+//    estimate with one correction (nb_m_rinv3_f64; FP64-pipe bound on GB300).
 //  * NB_F32C: over all bodies of a large system, the symmetric FP32 pair kernel of
 //    nb_pair_sym.cu (each unordered pair once, added to both bodies); otherwise (target ranges,
 //    small systems) the one-sided FP32-compensated pair kernel of nb_pair.cuh (scalar FP32 pair
@@ -184,23 +186,34 @@ naive_f64_targets_kernel(const double* __restrict__ m, const double* __restrict_
 // ---------------------------------------------------------------------------------------------
 int g_naive_pair_cfg = 0;  // tile configuration (nb_naive_set_pair_config)
 // Symmetric kernel (nb_pair_sym.cu) for full target ranges (nb_naive_set_symmetric): mode 0
-// never, 1 automatic, 2 always; and its configuration.
+// never, 1 automatic, 2 always; and its FP32 and FP64 shapes.
 int g_naive_sym_mode = 1;
 int g_naive_sym_cfg = 0;
-// Automatic selection wants at least this many units per persistent CTA (the one-sided kernel
-// spreads small systems better) and j-side partials (12 bytes per unit and tile body, about
-// 6 n^2 / IB bytes in all) below the cap.
+int g_naive_sym64_cfg = 0;
+// Automatic selection wants at least this many units per persistent CTA (the one-sided kernels
+// spread small systems better) and j-side partials (3 values per unit and tile body) below the
+// cap.
 constexpr uint64_t SYM_MIN_UNITS_PER_CTA = 8;
 constexpr size_t SYM_PART_CAP_BYTES = (size_t)4 << 30;
 
-nb_status naive_f32c_sym(nb_ctx* ctx, int cfg, const nb::SymHostPlan& hp, const double* m,
-                         const double* x, const double* y, const double* z, double* ax,
-                         double* ay, double* az, double G, double eps2, cudaStream_t stream) {
+// Runs the symmetric kernel for the whole system when the mode and the plan allow it; *done
+// tells whether it did.
+nb_status naive_sym(nb_ctx* ctx, bool f64, const double* m, const double* x, const double* y,
+                    const double* z, double* ax, double* ay, double* az, uint32_t n, double G,
+                    double eps2, cudaStream_t stream, bool* done) {
+    *done = false;
+    if (g_naive_sym_mode == 0) return NB_OK;
+    const int cfg = f64 ? g_naive_sym64_cfg : g_naive_sym_cfg;
+    nb::SymHostPlan hp;
+    NB_TRY(nb::sym_host_plan(f64, cfg, &n, 1, ctx->sm_count, &hp));
+    const size_t pj_bytes = nb::sym_part_j_bytes(f64, cfg, hp.units);
+    if (g_naive_sym_mode == 1 &&
+        (hp.units < SYM_MIN_UNITS_PER_CTA * hp.ctas || pj_bytes > SYM_PART_CAP_BYTES))
+        return NB_OK;
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t table_bytes = al(2 * sizeof(nbsym::SymSys));
-    const size_t src_bytes = al((size_t)hp.n_records * sizeof(float4));
-    const size_t pi_bytes = al(nb::sym_part_i_floats(cfg, hp.ctas, hp.n_blocks) * sizeof(float));
-    const size_t pj_bytes = nb::sym_part_j_floats(cfg, hp.units) * sizeof(float);
+    const size_t src_bytes = al((size_t)hp.n_records * nb::sym_record_bytes(f64));
+    const size_t pi_bytes = al(nb::sym_part_i_bytes(f64, cfg, hp.ctas, hp.n_blocks));
     void* base = nullptr;
     NB_TRY(nb::scratch(ctx, NB_SCRATCH_PAIR_SYM, table_bytes + src_bytes + pi_bytes + pj_bytes,
                        &base));
@@ -215,23 +228,19 @@ nb_status naive_f32c_sym(nb_ctx* ctx, int cfg, const nb::SymHostPlan& hp, const 
     S.n_records = hp.n_records;
     S.units = hp.units;
     b += table_bytes;
-    return nb::sym_launch(cfg, S, m, x, y, z, G, eps2, (float4*)b, (float*)(b + src_bytes),
-                          (float*)(b + src_bytes + pi_bytes), ax, ay, az, ctx->dev_error, stream);
+    *done = true;
+    return nb::sym_launch(f64, cfg, S, m, x, y, z, G, eps2, b, b + src_bytes,
+                          b + src_bytes + pi_bytes, ax, ay, az, ctx->dev_error, stream);
 }
 
 nb_status naive_f32c(nb_ctx* ctx, const double* m, const double* x, const double* y,
                      const double* z, double* ax, double* ay, double* az, uint32_t n,
                      uint32_t i_begin, uint32_t i_end, double G, double eps2,
                      cudaStream_t stream) {
-    if (i_begin == 0 && i_end == n && g_naive_sym_mode != 0) {
-        const int scfg = g_naive_sym_cfg;
-        nb::SymHostPlan hp;
-        NB_TRY(nb::sym_host_plan(scfg, &n, 1, ctx->sm_count, &hp));
-        const bool use =
-            g_naive_sym_mode == 2 ||
-            (hp.units >= SYM_MIN_UNITS_PER_CTA * hp.ctas &&
-             nb::sym_part_j_floats(scfg, hp.units) * sizeof(float) <= SYM_PART_CAP_BYTES);
-        if (use) return naive_f32c_sym(ctx, scfg, hp, m, x, y, z, ax, ay, az, G, eps2, stream);
+    if (i_begin == 0 && i_end == n) {
+        bool done = false;
+        NB_TRY(naive_sym(ctx, false, m, x, y, z, ax, ay, az, n, G, eps2, stream, &done));
+        if (done) return NB_OK;
     }
     const int cfg = g_naive_pair_cfg;
     const nb::PairConfig& C = nb::kPairConfigs[cfg];
@@ -426,6 +435,11 @@ nb_status naive_dispatch(nb_ctx* ctx, const double* m, const double* x, const do
                 m, x, y, z, ax, ay, az, n, i_begin, i_end, G, eps2, n, nullptr);
             return nb::check_launch("naive_f64_kernel<ieee>");
         case NB_F64: {
+            if (i_begin == 0 && i_end == n) {
+                bool done = false;
+                NB_TRY(naive_sym(ctx, true, m, x, y, z, ax, ay, az, n, G, eps2, stream, &done));
+                if (done) return NB_OK;
+            }
             const int blocks = nb::ceil_div(n_t, F64_THREADS);
             uint32_t chunks = 1, chunk = n;
             choose_chunks(ctx, blocks, n, F64_THREADS, &chunks, &chunk);
@@ -488,13 +502,16 @@ nb_status nb_naive_set_pair_config(int config) {
     return NB_OK;
 }
 
-nb_status nb_naive_set_symmetric(int mode, int config) {
+nb_status nb_naive_set_symmetric(int mode, int config_f32, int config_f64) {
     if (mode < 0 || mode > 2)
         return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_set_symmetric: mode %d", mode);
-    if (config < 0 || config >= nb::NB_SYM_CONFIGS)
-        return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_set_symmetric: config %d", config);
+    if (config_f32 < 0 || config_f32 >= nb::NB_SYM_CONFIGS || config_f64 < 0 ||
+        config_f64 >= nb::NB_SYM64_CONFIGS)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_set_symmetric: config %d / %d",
+                             config_f32, config_f64);
     g_naive_sym_mode = mode;
-    g_naive_sym_cfg = config;
+    g_naive_sym_cfg = config_f32;
+    g_naive_sym64_cfg = config_f64;
     return NB_OK;
 }
 

@@ -1,4 +1,5 @@
-// nb_pair_sym.cuh -- plan and launcher of the symmetric FP32 pair kernel (nb_pair_sym.cu).
+// nb_pair_sym.cuh -- plan and launcher of the symmetric pair kernel (nb_pair_sym.cu), FP32 with
+// compensated accumulation or FP64.
 #pragma once
 #include <vector>
 
@@ -7,9 +8,9 @@
 namespace nbsym {
 
 // One entry per system plus a closing entry with the totals (prefix sums): first unit, first
-// body in the FP64 arrays, first padded FP32 record and first I-block of system s. System s has
-// off[s+1] - off[s] bodies in boff[s+1] - boff[s] I-blocks of IB bodies (records padded to whole
-// I-blocks) and ceil(n / JT) j-tiles of JT bodies.
+// body in the FP64 arrays, first padded source record and first I-block of system s. System s
+// has off[s+1] - off[s] bodies in boff[s+1] - boff[s] I-blocks of IB bodies (records padded to
+// whole I-blocks) and ceil(n / JT) j-tiles of JT bodies.
 struct SymSys {
     uint64_t uoff;
     uint32_t off, poff, boff, pad;
@@ -32,17 +33,21 @@ __host__ __device__ __forceinline__ uint64_t row_off(uint32_t n_jt, uint32_t tpb
 
 namespace nb {
 
+// Tile shape: warps per CTA, bodies per lane, j-tile bodies.
 struct SymConfig {
     int warps, p, jt;
 };
-constexpr int NB_SYM_CONFIGS = 8;
+constexpr int NB_SYM_CONFIGS = 8;    // FP32 shapes
+constexpr int NB_SYM64_CONFIGS = 4;  // FP64 shapes
 extern const SymConfig kSymConfigs[NB_SYM_CONFIGS];
+extern const SymConfig kSym64Configs[NB_SYM64_CONFIGS];
 
-// Bodies per I-block of configuration cfg.
-inline uint32_t sym_ib(int cfg) { return 32u * kSymConfigs[cfg].warps * kSymConfigs[cfg].p; }
+// Bodies per I-block of a shape, and bytes per source record (16 FP32, 32 FP64).
+uint32_t sym_ib(bool f64, int cfg);
+size_t sym_record_bytes(bool f64);
 
-// Resident CTAs per SM of configuration cfg (also opts it into its dynamic shared memory).
-nb_status sym_ctas_per_sm(int cfg, int* out);
+// Resident CTAs per SM of a shape (also opts it into its dynamic shared memory).
+nb_status sym_ctas_per_sm(bool f64, int cfg, int* out);
 
 // Host side of a plan: the per-system table and the totals.
 struct SymHostPlan {
@@ -50,17 +55,18 @@ struct SymHostPlan {
     uint64_t units = 0;
     uint32_t n_total = 0, n_records = 0, n_blocks = 0, ctas = 0;
 };
-nb_status sym_host_plan(int cfg, const uint32_t* counts, uint32_t n_systems, int sm_count,
-                        SymHostPlan* out);
-// Scratch of a plan: FP32 records (n_records float4), i-side and j-side partials (floats).
-size_t sym_part_i_floats(int cfg, uint32_t ctas, uint32_t n_blocks);
-size_t sym_part_j_floats(int cfg, uint64_t units);
+nb_status sym_host_plan(bool f64, int cfg, const uint32_t* counts, uint32_t n_systems,
+                        int sm_count, SymHostPlan* out);
+// Scratch of a plan: i-side and j-side partials (bytes); records take
+// n_records * sym_record_bytes(f64).
+size_t sym_part_i_bytes(bool f64, int cfg, uint32_t ctas, uint32_t n_blocks);
+size_t sym_part_j_bytes(bool f64, int cfg, uint64_t units);
 // Writes the device table of a single-system plan (two entries) with a kernel.
 nb_status sym_single_table(nbsym::SymSys* sys, const SymHostPlan& hp, cudaStream_t stream);
 // Launches prepare + symmetric pair kernel + combine for a plan whose device table is filled.
-nb_status sym_launch(int cfg, const nbsym::SymPlan& S, const double* m, const double* x,
-                     const double* y, const double* z, double G, double eps2, float4* src,
-                     float* part_i, float* part_j, double* ax, double* ay, double* az,
+nb_status sym_launch(bool f64, int cfg, const nbsym::SymPlan& S, const double* m, const double* x,
+                     const double* y, const double* z, double G, double eps2, void* src,
+                     void* part_i, void* part_j, double* ax, double* ay, double* az,
                      uint32_t* err_word, cudaStream_t stream);
 
 }  // namespace nb

@@ -2,9 +2,9 @@
 unordered pair evaluated once and added to both bodies) against the CPU oracle restating
 NaiveAlgorithm.cpp:262-360, through the C ABI.
 
-Tolerances (those of the one-sided NB_F32C kernel): per-body relative error median <= 1e-5 and
-max <= 1e-3 on Plummer spheres (eps = 1e-3), median <= 1e-4 on the heliocentric disc; repeated
-calls bit-identical (fixed combine order).
+Tolerances (those of the one-sided kernels): NB_F32C per-body relative error median <= 1e-5 and
+max <= 1e-3 on Plummer spheres (eps = 1e-3), median <= 1e-4 on the heliocentric disc; NB_F64
+per-body relative error <= 1e-12; repeated calls bit-identical (fixed combine order).
 """
 
 import numpy as np
@@ -26,18 +26,18 @@ def ctx():
     c.close()
 
 
-def run_f32c(ctx, d, eps2, mode, config=0):
+def run_f32c(ctx, d, eps2, mode, config=0, precision="f32c", config_f64=0):
     import torch
     from nbody.lib import SYM_AUTO, set_naive_symmetric
     t = {k: dev(d[k]) for k in ("m", "x", "y", "z")}
     n = len(d["m"])
     a = [torch.full((n,), float("nan"), dtype=torch.float64, device="cuda") for _ in range(3)]
     try:
-        set_naive_symmetric(mode, config)
-        ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, d["G"], eps2, "f32c")
+        set_naive_symmetric(mode, config, config_f64)
+        ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, d["G"], eps2, precision)
         ctx.sync()
     finally:
-        set_naive_symmetric(SYM_AUTO, 0)
+        set_naive_symmetric(SYM_AUTO, 0, 0)
     return tuple(host(v) for v in a)
 
 
@@ -95,3 +95,34 @@ def test_automatic_selection_large(ctx):
     ref = [host(v) for v in ref]
     err = rel_err(*(v[targets] for v in sym), *ref)
     assert np.median(err) <= 1e-5 and err.max() <= 1e-3, (np.median(err), err.max())
+
+
+@pytest.mark.parametrize("config_f64", [0, 1, 2, 3])
+@pytest.mark.parametrize("kind,n,eps2", [("disc", 16384, 1e-22), ("plummer", 3000, 1e-6),
+                                         ("disc", 1, 1e-22), ("plummer", 129, 1e-6),
+                                         ("disc", 777, 1e-22)])
+def test_symmetric_f64_within_1e12(ctx, kind, n, eps2, config_f64):
+    from nbody.lib import SYM_ALWAYS
+    if config_f64 and n != 3000:
+        pytest.skip("other sizes run with the default FP64 shape only")
+    d = bodies(kind, n, seed=31)
+    got = run_f32c(ctx, d, eps2, SYM_ALWAYS, precision="f64", config_f64=config_f64)
+    if n == 1:
+        assert all(np.all(g == 0) for g in got)
+        return
+    ref = oracle.naive_accel(d["m"], d["x"], d["y"], d["z"], d["G"], eps2)
+    err = rel_err(*got, *ref)
+    assert err.max() <= 1e-12, err.max()
+
+
+def test_symmetric_f64_deterministic_and_selected(ctx):
+    """At 16,384 bodies the automatic mode takes the FP64 symmetric kernel (its result equals the
+    forced one bit for bit, and differs from the one-sided kernel's by rounding only)."""
+    from nbody.lib import SYM_ALWAYS, SYM_AUTO, SYM_NEVER
+    d = bodies("disc", 16384, seed=2)
+    auto = run_f32c(ctx, d, 1e-22, SYM_AUTO, precision="f64")
+    forced = run_f32c(ctx, d, 1e-22, SYM_ALWAYS, precision="f64")
+    one = run_f32c(ctx, d, 1e-22, SYM_NEVER, precision="f64")
+    for a, f in zip(auto, forced):
+        np.testing.assert_array_equal(a, f)
+    assert rel_err(*auto, *one).max() <= 2e-12
