@@ -6,6 +6,9 @@
     python n-body-simulation_gb300/nbody/cases.py sym [N] [config]
         the same three evaluations with the symmetric kernel (pair_sym_kernel), configuration
         `config`
+    python n-body-simulation_gb300/nbody/cases.py sym64 [N] [config]
+        seeded heliocentric disc, three FP64 naive evaluations (NB_F64) with the FP64 form of the
+        symmetric kernel, FP64 configuration `config`
     python n-body-simulation_gb300/nbody/cases.py learned [N] [log10_tau] [pairs]
         seeded disc + Plummer mix: labelled pairs and a short training of the opening network,
         then three learned traversals (bh_learned_kernel) at threshold tau
@@ -41,6 +44,21 @@ def pair_case(n: int = 262144, config: int = 0, symmetric: bool = False):
     acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
     for _ in range(3):
         ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, 1.0, 1e-6, "f32c")
+    ctx.sync()
+
+
+def sym64_case(n: int = 65536, config: int = 0):
+    import torch
+
+    from nbody import generators, learned
+    from nbody.lib import SYM_ALWAYS, Context, set_naive_symmetric
+    ctx = Context(0)
+    set_naive_symmetric(SYM_ALWAYS, 0, config)
+    d = generators.heliocentric_disc(n, 1)
+    t = learned.device_system(d)
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    for _ in range(3):
+        ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, d["G"], learned.EPS2, "f64")
     ctx.sync()
 
 
@@ -82,13 +100,15 @@ def df64_case(n: int = 262144):
 
 
 def main(argv):
-    if not argv or argv[0] not in ("pair", "sym", "learned", "df64"):
+    if not argv or argv[0] not in ("pair", "sym", "sym64", "learned", "df64"):
         print(__doc__)
         return 2
     args = argv[1:]
     if argv[0] in ("pair", "sym"):
         pair_case(int(args[0]) if args else 262144, int(args[1]) if len(args) > 1 else 0,
                   argv[0] == "sym")
+    elif argv[0] == "sym64":
+        sym64_case(int(args[0]) if args else 65536, int(args[1]) if len(args) > 1 else 0)
     elif argv[0] == "df64":
         df64_case(int(args[0]) if args else 262144)
     else:
