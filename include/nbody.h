@@ -106,8 +106,9 @@ nb_status nb_naive_set_pair_config(int config);
  * most 4 GiB), 2 = always for full ranges. config_f32: 0..NB_SYM_CONFIG_COUNT-1, FP32 tile shapes
  * (warps, bodies per lane, j-tile) = (8,12,128) (default), (4,12,256), (4,12,128), (4,16,128),
  * (8,8,256), (4,8,256), (8,6,256), (2,12,128); config_f64: 0..NB_SYM64_CONFIG_COUNT-1, FP64
- * shapes (4,2,64) (default), (4,4,64), (8,2,64), (4,2,128). Process-wide; nb_naive_accel_range
- * with a partial range always uses the one-sided kernels. */
+ * shapes (4,2,64), (4,4,64), (8,2,64), (4,2,128), used in mode 2 (in mode 1 the library takes
+ * the largest FP64 I-block that still fills the GPU). Process-wide; nb_naive_accel_range with a
+ * partial range always uses the one-sided kernels. */
 #define NB_SYM_CONFIG_COUNT 8
 #define NB_SYM64_CONFIG_COUNT 4
 nb_status nb_naive_set_symmetric(int mode, int config_f32, int config_f64);

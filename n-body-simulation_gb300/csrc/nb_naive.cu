@@ -203,9 +203,20 @@ nb_status naive_sym(nb_ctx* ctx, bool f64, const double* m, const double* x, con
                     double eps2, cudaStream_t stream, bool* done) {
     *done = false;
     if (g_naive_sym_mode == 0) return NB_OK;
-    const int cfg = f64 ? g_naive_sym64_cfg : g_naive_sym_cfg;
+    int cfg = f64 ? g_naive_sym64_cfg : g_naive_sym_cfg;
     nb::SymHostPlan hp;
-    NB_TRY(nb::sym_host_plan(f64, cfg, &n, 1, ctx->sm_count, &hp));
+    if (f64 && g_naive_sym_mode == 1) {
+        // automatic FP64 shape: the largest I-block that still gives every persistent CTA
+        // enough units (fewer partials: 24 bytes per unit and tile body)
+        static const int kByBlock[] = {1, 0};  // (4,4,64) IB 512, then (4,2,64) IB 256
+        for (int c : kByBlock) {
+            NB_TRY(nb::sym_host_plan(true, c, &n, 1, ctx->sm_count, &hp));
+            cfg = c;
+            if (hp.units >= SYM_MIN_UNITS_PER_CTA * hp.ctas) break;
+        }
+    } else {
+        NB_TRY(nb::sym_host_plan(f64, cfg, &n, 1, ctx->sm_count, &hp));
+    }
     const size_t pj_bytes = nb::sym_part_j_bytes(f64, cfg, hp.units);
     if (g_naive_sym_mode == 1 &&
         (hp.units < SYM_MIN_UNITS_PER_CTA * hp.ctas || pj_bytes > SYM_PART_CAP_BYTES))
