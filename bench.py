@@ -519,6 +519,7 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
     ms = timed(lambda: ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, dd["G"], EPS2, "df64"),
                5)
     out["naive_df64_disc_16384"] = {
+        "kernel": "pair_sym_df_kernel (each unordered pair once, added to both bodies)",
         "ms_per_eval": ms, "gpairs_per_s": n * n / (ms * 1e-3) / 1e9,
         "arithmetic": "double-float (FP32 pairs) on the FP32 pipe, FP64-accurate to ~1e-14"}
     for name, fn in (("precision_form_naive_f32c_plummer_262144", workloads.precision_form),

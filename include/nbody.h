@@ -98,20 +98,23 @@ nb_status nb_naive_accel_targets(nb_ctx* ctx, const double* m, const double* x, 
 #define NB_PAIR_CONFIG_COUNT 8
 nb_status nb_naive_set_pair_config(int config);
 
-/* Symmetric pair kernel for nb_naive_accel(NB_F32C and NB_F64) over all bodies of a system (no
- * reference counterpart; the reference evaluates every ordered pair, NaiveAlgorithm.cpp:318-346):
- * each unordered pair is evaluated once and added to both bodies, per-body sums combined in a
- * fixed order (deterministic; FP32 sums compensated). mode: 0 = never (always the one-sided
- * kernels), 1 = automatic (default: systems large enough to fill the GPU, partial buffers of at
- * most 4 GiB), 2 = always for full ranges. config_f32: 0..NB_SYM_CONFIG_COUNT-1, FP32 tile shapes
- * (warps, bodies per lane, j-tile) = (8,12,128) (default), (4,12,256), (4,12,128), (4,16,128),
- * (8,8,256), (4,8,256), (8,6,256), (2,12,128); config_f64: 0..NB_SYM64_CONFIG_COUNT-1, FP64
- * shapes (4,2,64), (4,4,64), (8,2,64), (4,2,128), used in mode 2 (in mode 1 the library takes
- * the largest FP64 I-block that still fills the GPU). Process-wide; nb_naive_accel_range with a
- * partial range always uses the one-sided kernels. */
+/* Symmetric pair kernel for nb_naive_accel (NB_F32C, NB_F64 and NB_DF64) over all bodies of a
+ * system (no reference counterpart; the reference evaluates every ordered pair,
+ * NaiveAlgorithm.cpp:318-346): each unordered pair is evaluated once and added to both bodies,
+ * per-body sums combined in a fixed order (deterministic; FP32 sums compensated). mode: 0 = never
+ * (always the one-sided kernels), 1 = automatic (default: systems large enough to fill the GPU,
+ * partial buffers of at most 4 GiB), 2 = always for full ranges. Tile shapes (warps, bodies per
+ * lane, j-tile): config_f32 0..NB_SYM_CONFIG_COUNT-1 = (8,12,128) (default), (4,12,256),
+ * (4,12,128), (4,16,128), (8,8,256), (4,8,256), (8,6,256), (2,12,128); config_f64
+ * 0..NB_SYM64_CONFIG_COUNT-1 = (4,2,64), (4,4,64), (8,2,64), (4,2,128); config_df
+ * 0..NB_SYMDF_CONFIG_COUNT-1 = (4,2,64), (4,4,64). In mode 1 the FP64 and double-float shapes
+ * are chosen by the library (FP64: the larger I-block when it still fills the GPU; double-float:
+ * the faster (4,2,64) unless its partials exceed the cap). Process-wide; nb_naive_accel_range
+ * with a partial range always uses the one-sided kernels. */
 #define NB_SYM_CONFIG_COUNT 8
 #define NB_SYM64_CONFIG_COUNT 4
-nb_status nb_naive_set_symmetric(int mode, int config_f32, int config_f64);
+#define NB_SYMDF_CONFIG_COUNT 2
+nb_status nb_naive_set_symmetric(int mode, int config_f32, int config_f64, int config_df);
 
 /* ---------------------------------------------------------------------------------------------
  * Batched ensembles (the batching form of the method; the reference simulates one system).

@@ -76,7 +76,7 @@ nb_status host_plan(const nb_batch* b, int cfg, int sm_count, HostPlan* hp) {
 nb_status apply_config(nb_batch* b, int cfg, int sm_count) {
     if (is_sym(cfg)) {
         nb::SymHostPlan sp;
-        NB_TRY(nb::sym_host_plan(false, cfg - nb::NB_PAIR_CONFIGS, b->counts.data(),
+        NB_TRY(nb::sym_host_plan(nb::SYM_F32, cfg - nb::NB_PAIR_CONFIGS, b->counts.data(),
                                  b->n_systems, sm_count, &sp));
         NB_CUDA_TRY(cudaMemcpy(b->sym_table, sp.sys.data(), sp.sys.size() * sizeof(nbsym::SymSys),
                                cudaMemcpyHostToDevice));
@@ -104,8 +104,8 @@ nb_status batch_accel(nb_ctx* ctx, nb_batch* b, const double* m, const double* x
                       const double* z, double* ax, double* ay, double* az, double G, double eps2,
                       cudaStream_t s) {
     if (is_sym(b->cfg))
-        return nb::sym_launch(false, b->cfg - nb::NB_PAIR_CONFIGS, b->sym_plan, m, x, y, z, G,
-                              eps2,
+        return nb::sym_launch(nb::SYM_F32, b->cfg - nb::NB_PAIR_CONFIGS, b->sym_plan, m, x, y,
+                              z, G, eps2,
                               b->sym_src, b->sym_part_i, b->sym_part_j, ax, ay, az,
                               ctx->dev_error, s);
     if (b->plan.units == 0) return NB_OK;
@@ -155,14 +155,14 @@ nb_status nb_batch_create(nb_ctx* ctx, uint32_t n_systems, const uint32_t* count
     for (int c = 0; c < nb::NB_SYM_CONFIGS; ++c) {
         nb::SymHostPlan sp;
         nb_status st =
-            nb::sym_host_plan(false, c, b->counts.data(), n_systems, ctx->sm_count, &sp);
+            nb::sym_host_plan(nb::SYM_F32, c, b->counts.data(), n_systems, ctx->sm_count, &sp);
         if (st != NB_OK) {
             delete b;
             return st;
         }
         sym_records = std::max(sym_records, (size_t)sp.n_records);
-        sym_pi = std::max(sym_pi, nb::sym_part_i_bytes(false, c, sp.ctas, sp.n_blocks));
-        sym_pj = std::max(sym_pj, nb::sym_part_j_bytes(false, c, sp.units));
+        sym_pi = std::max(sym_pi, nb::sym_part_i_bytes(nb::SYM_F32, c, sp.ctas, sp.n_blocks));
+        sym_pj = std::max(sym_pj, nb::sym_part_j_bytes(nb::SYM_F32, c, sp.units));
     }
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t ns = n_systems + 1;

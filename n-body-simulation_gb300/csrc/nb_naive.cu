@@ -14,7 +14,8 @@
 //    small systems) the one-sided FP32-compensated pair kernel of nb_pair.cuh (scalar FP32 pair
 //    math, TwoSum accumulation, stream-K persistent CTAs, cp.async.bulk j-tiles behind bounded
 //    mbarrier waits), run as a batch of one system.
-//  * NB_DF64: double-float pair math on the FP32 pipe (FP64-accurate to ~1e-14).
+//  * NB_DF64: double-float pair math on the FP32 pipe (FP64-accurate to ~1e-14); over all bodies
+//    of a large system the double-float form of the symmetric pair kernel.
 #include "nb_internal.cuh"
 #include "nb_pair.cuh"
 #include "nb_pair_sym.cuh"
@@ -186,45 +187,52 @@ naive_f64_targets_kernel(const double* __restrict__ m, const double* __restrict_
 // ---------------------------------------------------------------------------------------------
 int g_naive_pair_cfg = 0;  // tile configuration (nb_naive_set_pair_config)
 // Symmetric kernel (nb_pair_sym.cu) for full target ranges (nb_naive_set_symmetric): mode 0
-// never, 1 automatic, 2 always; and its FP32 and FP64 shapes.
+// never, 1 automatic, 2 always; and its FP32, FP64 and double-float shapes.
 int g_naive_sym_mode = 1;
-int g_naive_sym_cfg = 0;
-int g_naive_sym64_cfg = 0;
+int g_naive_sym_cfg[3] = {0, 0, 0};
 // Automatic selection wants at least this many units per persistent CTA (the one-sided kernels
 // spread small systems better) and j-side partials (3 values per unit and tile body) below the
 // cap.
 constexpr uint64_t SYM_MIN_UNITS_PER_CTA = 8;
 constexpr size_t SYM_PART_CAP_BYTES = (size_t)4 << 30;
 
-// Runs the symmetric kernel for the whole system when the mode and the plan allow it; *done
-// tells whether it did.
-nb_status naive_sym(nb_ctx* ctx, bool f64, const double* m, const double* x, const double* y,
+// Runs the symmetric kernel of arithmetic form `form` (nb::SymForm) for the whole system when
+// the mode and the plan allow it; *done tells whether it did.
+nb_status naive_sym(nb_ctx* ctx, int form, const double* m, const double* x, const double* y,
                     const double* z, double* ax, double* ay, double* az, uint32_t n, double G,
                     double eps2, cudaStream_t stream, bool* done) {
     *done = false;
     if (g_naive_sym_mode == 0) return NB_OK;
-    int cfg = f64 ? g_naive_sym64_cfg : g_naive_sym_cfg;
-    nb::SymHostPlan hp;
-    if (f64 && g_naive_sym_mode == 1) {
-        // automatic FP64 shape: the largest I-block that still gives every persistent CTA
-        // enough units (fewer partials: 24 bytes per unit and tile body)
-        static const int kByBlock[] = {1, 0};  // (4,4,64) IB 512, then (4,2,64) IB 256
-        for (int c : kByBlock) {
-            NB_TRY(nb::sym_host_plan(true, c, &n, 1, ctx->sm_count, &hp));
-            cfg = c;
-            if (hp.units >= SYM_MIN_UNITS_PER_CTA * hp.ctas) break;
-        }
-    } else {
-        NB_TRY(nb::sym_host_plan(f64, cfg, &n, 1, ctx->sm_count, &hp));
+    // candidate shapes: the configured one, except in the automatic mode of the FP64 and
+    // double-float forms, where shape 1 is (4,4,64) with 512-body I-blocks and shape 0 (4,2,64)
+    // with 256: FP64 prefers the larger I-block (same speed, half the partials: 24 bytes per
+    // unit and tile body), double-float the smaller one (faster: fewer registers per thread)
+    int cand[2] = {g_naive_sym_cfg[form], -1};
+    if (g_naive_sym_mode == 1 && form == nb::SYM_F64) {
+        cand[0] = 1;
+        cand[1] = 0;
+    } else if (g_naive_sym_mode == 1 && form == nb::SYM_DF) {
+        cand[0] = 0;
+        cand[1] = 1;
     }
-    const size_t pj_bytes = nb::sym_part_j_bytes(f64, cfg, hp.units);
-    if (g_naive_sym_mode == 1 &&
-        (hp.units < SYM_MIN_UNITS_PER_CTA * hp.ctas || pj_bytes > SYM_PART_CAP_BYTES))
-        return NB_OK;
+    int cfg = -1;
+    nb::SymHostPlan hp;
+    size_t pj_bytes = 0;
+    for (int c : cand) {
+        if (c < 0) break;
+        NB_TRY(nb::sym_host_plan(form, c, &n, 1, ctx->sm_count, &hp));
+        pj_bytes = nb::sym_part_j_bytes(form, c, hp.units);
+        if (g_naive_sym_mode == 2 || (hp.units >= SYM_MIN_UNITS_PER_CTA * hp.ctas &&
+                                      pj_bytes <= SYM_PART_CAP_BYTES)) {
+            cfg = c;
+            break;
+        }
+    }
+    if (cfg < 0) return NB_OK;
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t table_bytes = al(2 * sizeof(nbsym::SymSys));
-    const size_t src_bytes = al((size_t)hp.n_records * nb::sym_record_bytes(f64));
-    const size_t pi_bytes = al(nb::sym_part_i_bytes(f64, cfg, hp.ctas, hp.n_blocks));
+    const size_t src_bytes = al((size_t)hp.n_records * nb::sym_record_bytes(form));
+    const size_t pi_bytes = al(nb::sym_part_i_bytes(form, cfg, hp.ctas, hp.n_blocks));
     void* base = nullptr;
     NB_TRY(nb::scratch(ctx, NB_SCRATCH_PAIR_SYM, table_bytes + src_bytes + pi_bytes + pj_bytes,
                        &base));
@@ -240,7 +248,7 @@ nb_status naive_sym(nb_ctx* ctx, bool f64, const double* m, const double* x, con
     S.units = hp.units;
     b += table_bytes;
     *done = true;
-    return nb::sym_launch(f64, cfg, S, m, x, y, z, G, eps2, b, b + src_bytes,
+    return nb::sym_launch(form, cfg, S, m, x, y, z, G, eps2, b, b + src_bytes,
                           b + src_bytes + pi_bytes, ax, ay, az, ctx->dev_error, stream);
 }
 
@@ -250,7 +258,7 @@ nb_status naive_f32c(nb_ctx* ctx, const double* m, const double* x, const double
                      cudaStream_t stream) {
     if (i_begin == 0 && i_end == n) {
         bool done = false;
-        NB_TRY(naive_sym(ctx, false, m, x, y, z, ax, ay, az, n, G, eps2, stream, &done));
+        NB_TRY(naive_sym(ctx, nb::SYM_F32, m, x, y, z, ax, ay, az, n, G, eps2, stream, &done));
         if (done) return NB_OK;
     }
     const int cfg = g_naive_pair_cfg;
@@ -448,7 +456,8 @@ nb_status naive_dispatch(nb_ctx* ctx, const double* m, const double* x, const do
         case NB_F64: {
             if (i_begin == 0 && i_end == n) {
                 bool done = false;
-                NB_TRY(naive_sym(ctx, true, m, x, y, z, ax, ay, az, n, G, eps2, stream, &done));
+                NB_TRY(naive_sym(ctx, nb::SYM_F64, m, x, y, z, ax, ay, az, n, G, eps2, stream,
+                                 &done));
                 if (done) return NB_OK;
             }
             const int blocks = nb::ceil_div(n_t, F64_THREADS);
@@ -470,8 +479,15 @@ nb_status naive_dispatch(nb_ctx* ctx, const double* m, const double* x, const do
         }
         case NB_F32C:
             return naive_f32c(ctx, m, x, y, z, ax, ay, az, n, i_begin, i_end, G, eps2, stream);
-        case NB_DF64:
+        case NB_DF64: {
+            if (i_begin == 0 && i_end == n) {
+                bool done = false;
+                NB_TRY(naive_sym(ctx, nb::SYM_DF, m, x, y, z, ax, ay, az, n, G, eps2, stream,
+                                 &done));
+                if (done) return NB_OK;
+            }
             return naive_df64(ctx, m, x, y, z, ax, ay, az, n, i_begin, i_end, G, eps2, stream);
+        }
         default:
             return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_accel: unknown precision %d",
                                  (int)prec);
@@ -513,16 +529,16 @@ nb_status nb_naive_set_pair_config(int config) {
     return NB_OK;
 }
 
-nb_status nb_naive_set_symmetric(int mode, int config_f32, int config_f64) {
+nb_status nb_naive_set_symmetric(int mode, int config_f32, int config_f64, int config_df) {
     if (mode < 0 || mode > 2)
         return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_set_symmetric: mode %d", mode);
-    if (config_f32 < 0 || config_f32 >= nb::NB_SYM_CONFIGS || config_f64 < 0 ||
-        config_f64 >= nb::NB_SYM64_CONFIGS)
-        return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_set_symmetric: config %d / %d",
-                             config_f32, config_f64);
+    const int cfg[3] = {config_f32, config_f64, config_df};
+    for (int f = 0; f < 3; ++f)
+        if (cfg[f] < 0 || cfg[f] >= nb::sym_config_count(f))
+            return nb::set_error(NB_ERR_INVALID_ARG, "nb_naive_set_symmetric: config %d of form %d",
+                                 cfg[f], f);
     g_naive_sym_mode = mode;
-    g_naive_sym_cfg = config_f32;
-    g_naive_sym64_cfg = config_f64;
+    for (int f = 0; f < 3; ++f) g_naive_sym_cfg[f] = cfg[f];
     return NB_OK;
 }
 

@@ -10,6 +10,10 @@
 //    the hardware rsqrt estimate with one correction of its cube (6 FP64 operations), 20 FP64
 //    operations per unordered pair against 32 for the two ordered pairs; G applied once at the end
 //    as in NaiveAlgorithm.cpp:348-351.
+//  * Double-float (nb_naive_accel NB_DF64 over whole systems): positions relative to the system's
+//    first body as exact triple-floats and G*m as a double-float; the separation, r^2 + eps^2,
+//    1/r and r^-3 in double-float arithmetic are shared by the two bodies, only the mass products,
+//    the force terms and the compensated sums are per body (pair_sym_df_kernel).
 //
 // Decomposition: per system, bodies in I-blocks of IB = 32 W P (W warps, P bodies per lane) and
 // j-tiles of JT; I-block a owns the j-tiles from its own first tile to the system's last, and the
@@ -133,6 +137,34 @@ __global__ void sym_single_table_kernel(SymSys* sys, uint32_t n, uint32_t nb, ui
                                         uint64_t units) {
     sys[0] = SymSys{0, 0, 0, 0, 0};
     sys[1] = SymSys{units, n, records, nb, 0};
+}
+
+// Double-float source record: the position minus the system's first body as exact
+// triple-floats, G*m as a double-float.
+struct __align__(16) RecTF {
+    float xh, xm, xl, yh, ym, yl, zh, zm, zl, gh, gl, pad;
+};
+
+__global__ void sym_prepare_tf_kernel(SymPlan P, const double* __restrict__ m,
+                                      const double* __restrict__ x, const double* __restrict__ y,
+                                      const double* __restrict__ z, double G,
+                                      RecTF* __restrict__ out) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P.n_records) return;
+    const uint32_t s = last_le(P.n_systems, r, [&](uint32_t k) { return P.sys[k].poff; });
+    const SymSys A = P.sys[s], B = P.sys[s + 1];
+    const uint32_t t = r - A.poff;
+    RecTF o{1e18f, 0.f, 0.f, 1e18f, 0.f, 0.f, 1e18f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (t < B.off - A.off) {
+        const uint32_t b = A.off + t, a0 = A.off;
+        tf_split_diff(x[b], x[a0], o.xh, o.xm, o.xl);
+        tf_split_diff(y[b], y[a0], o.yh, o.ym, o.yl);
+        tf_split_diff(z[b], z[a0], o.zh, o.zm, o.zl);
+        const double gm = G * m[b];
+        o.gh = (float)gm;
+        o.gl = (float)(gm - (double)o.gh);
+    }
+    out[r] = o;
 }
 
 template <typename R>
@@ -333,6 +365,190 @@ pair_sym_kernel(SymPlan S, const typename RecOf<R>::type* __restrict__ src, R ep
     }
 }
 
+// Double-float form: the decomposition, copies and partial layout of the FP64 form (FP64 i
+// totals per row segment, FP64 j partials per unit); per pair the arithmetic of the one-sided
+// double-float kernel (exact triple-float separation, r^2 + eps^2 with TwoSums, 1/r from the
+// hardware estimate with an error-free correction, products in double-float), once for both
+// bodies; per-tile Neumaier-compensated FP32 sums folded into the FP64 totals.
+template <int W, int P, int JT>
+constexpr size_t sym_df_smem_bytes() {
+    return 2 * JT * sizeof(RecTF) + (size_t)2 * W * 3 * JT * sizeof(double);
+}
+
+template <int W, int P, int JT>
+__global__ void __launch_bounds__(32 * W)
+pair_sym_df_kernel(SymPlan S, const RecTF* __restrict__ src, float e2h, float e2l,
+                   double* __restrict__ part_i, double* __restrict__ part_j,
+                   uint32_t* __restrict__ err_word) {
+    constexpr int THREADS = 32 * W;
+    constexpr int IB = THREADS * P;
+    constexpr uint32_t TPB = IB / JT;
+    static_assert(IB % JT == 0 && JT % 32 == 0, "tile shape");
+    extern __shared__ __align__(128) unsigned char sym_smem[];
+    RecTF (*tile)[JT] = reinterpret_cast<RecTF (*)[JT]>(sym_smem);
+    double (*jacc)[W][3][JT] =
+        reinterpret_cast<double (*)[W][3][JT]>(sym_smem + 2 * JT * sizeof(RecTF));
+    __shared__ __align__(8) uint64_t full[2];
+
+    const uint32_t cta = blockIdx.x;
+    const uint64_t u0 = unit_begin(S, cta), u1 = unit_begin(S, cta + 1);
+    if (u0 >= u1) return;
+    if (threadIdx.x == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    uint64_t c_u = u0;
+    auto issue = [&](int buf) {
+        const Loc L = locate<TPB, JT>(S, c_u);
+        mbar_expect_tx(&full[buf], JT * (uint32_t)sizeof(RecTF));
+        bulk_g2s(&tile[buf][0], src + L.poff + (size_t)L.jt * JT, JT * (uint32_t)sizeof(RecTF),
+                 &full[buf]);
+        ++c_u;
+    };
+    if (threadIdx.x == 0) {
+        issue(0);
+        if (u0 + 1 < u1) issue(1);
+    }
+
+    const int th = threadIdx.x, lane = th & 31, w = th >> 5;
+    RecTF I[P];
+    double tx[P], ty[P], tz[P];
+    uint64_t u = u0;
+    uint32_t iter = 0;
+    bool failed = false;
+    while (u < u1 && !failed) {
+        const Loc L = locate<TPB, JT>(S, u);
+        const uint32_t a = L.a;
+        const uint64_t seg_end = min(u1, L.ubase + row_off(L.n_jt, TPB, a + 1));
+        uint32_t jt = L.jt;
+        const RecTF* isrc = src + L.poff + (size_t)a * IB + w * 32 * P + lane;
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            I[k] = isrc[k * 32];
+            tx[k] = ty[k] = tz[k] = 0.0;
+        }
+        for (; u < seg_end; ++u, ++iter, ++jt) {
+            const int buf = iter & 1;
+            const bool ok = mbar_wait(&full[buf], (iter >> 1) & 1);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            float ahx[P], alx[P], ahy[P], aly[P], ahz[P], alz[P];
+#pragma unroll
+            for (int k = 0; k < P; ++k) ahx[k] = alx[k] = ahy[k] = aly[k] = ahz[k] = alz[k] = 0.f;
+#pragma unroll 1
+            for (int g = 0; g < JT / 32; ++g) {
+                const RecTF* G4 = &tile[buf][g * 32];
+                // compensated sums of body (lane + s) mod 32 of the group
+                float jhx = 0.f, jlx = 0.f, jhy = 0.f, jly = 0.f, jhz = 0.f, jlz = 0.f;
+#pragma unroll 1
+                for (int s = 0; s < 32; ++s) {
+                    const RecTF J = G4[(lane + s) & 31];
+#pragma unroll
+                    for (int k = 0; k < P; ++k) {
+                        const nb_df dx = tf_diff(J.xh, J.xm, J.xl, I[k].xh, I[k].xm, I[k].xl);
+                        const nb_df dy = tf_diff(J.yh, J.ym, J.yl, I[k].yh, I[k].ym, I[k].yl);
+                        const nb_df dz = tf_diff(J.zh, J.zm, J.zl, I[k].zh, I[k].zm, I[k].zl);
+                        const nb_df sx = df_sqr(dx), sy = df_sqr(dy), sz = df_sqr(dz);
+                        nb_df c1 = df_two_sum(sx.h, sy.h);
+                        c1.l += sx.l + sy.l;
+                        nb_df c2 = df_two_sum(c1.h, sz.h);
+                        c2.l += c1.l + sz.l;
+                        nb_df c3 = df_two_sum(c2.h, e2h);
+                        c3.l += c2.l + e2l;
+                        const nb_df r2 = df_two_sum(c3.h, c3.l);
+                        const float y0 = nb_rsqrt_f32(r2.h);
+                        const float q = y0 * y0, qe = fmaf(y0, y0, -q);  // y0^2 = q + qe
+                        const float th2 = r2.h * q;
+                        float te = fmaf(r2.h, q, -th2);
+                        te = fmaf(r2.h, qe, te);
+                        te = fmaf(r2.l, q, te);
+                        const float e = (1.0f - th2) - te;
+                        const nb_df inv = df_fast_two_sum(y0, y0 * (e * fmaf(0.375f, e, 0.5f)));
+                        const nb_df inv3 = df_mul(df_sqr(inv), inv);
+                        const nb_df wj = df_mul(nb_df{J.gh, J.gl}, inv3);
+                        const nb_df wi = df_mul(nb_df{I[k].gh, I[k].gl}, inv3);
+                        // body i: + (x_j - x_i) G m_j / r^3
+                        nb_df t = df_mul(dx, wj);
+                        nb_df v = df_two_sum(ahx[k], t.h);
+                        ahx[k] = v.h;
+                        alx[k] += v.l + t.l;
+                        t = df_mul(dy, wj);
+                        v = df_two_sum(ahy[k], t.h);
+                        ahy[k] = v.h;
+                        aly[k] += v.l + t.l;
+                        t = df_mul(dz, wj);
+                        v = df_two_sum(ahz[k], t.h);
+                        ahz[k] = v.h;
+                        alz[k] += v.l + t.l;
+                        // body j: - (x_j - x_i) G m_i / r^3
+                        t = df_mul(dx, wi);
+                        v = df_two_sum(jhx, -t.h);
+                        jhx = v.h;
+                        jlx += v.l - t.l;
+                        t = df_mul(dy, wi);
+                        v = df_two_sum(jhy, -t.h);
+                        jhy = v.h;
+                        jly += v.l - t.l;
+                        t = df_mul(dz, wi);
+                        v = df_two_sum(jhz, -t.h);
+                        jhz = v.h;
+                        jlz += v.l - t.l;
+                    }
+                    // the sums of body (l + s + 1) mod 32 come from lane l + 1
+                    const int src_lane = (lane + 1) & 31;
+                    jhx = __shfl_sync(0xffffffffu, jhx, src_lane);
+                    jlx = __shfl_sync(0xffffffffu, jlx, src_lane);
+                    jhy = __shfl_sync(0xffffffffu, jhy, src_lane);
+                    jly = __shfl_sync(0xffffffffu, jly, src_lane);
+                    jhz = __shfl_sync(0xffffffffu, jhz, src_lane);
+                    jlz = __shfl_sync(0xffffffffu, jlz, src_lane);
+                }
+                // after 32 rotations lane l holds the sums of body l of the group
+                jacc[buf][w][0][g * 32 + lane] = (double)jhx + (double)jlx;
+                jacc[buf][w][1][g * 32 + lane] = (double)jhy + (double)jly;
+                jacc[buf][w][2][g * 32 + lane] = (double)jhz + (double)jlz;
+            }
+#pragma unroll
+            for (int k = 0; k < P; ++k) {
+                tx[k] += (double)ahx[k] + (double)alx[k];
+                ty[k] += (double)ahy[k] + (double)aly[k];
+                tz[k] += (double)ahz[k] + (double)alz[k];
+            }
+            __syncthreads();
+            if (jt >= (a + 1) * TPB) {  // above the diagonal: the j sums of this unit
+                double* out = part_j + u * 3 * JT;
+                for (int jl = th; jl < JT; jl += THREADS) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        double s = jacc[buf][0][c][jl];
+#pragma unroll
+                        for (int v = 1; v < W; ++v) s += jacc[buf][v][c][jl];
+                        out[c * JT + jl] = s;
+                    }
+                }
+            }
+            if (threadIdx.x == 0 && u + 2 < u1) issue(buf);  // the cursor is at u + 2
+        }
+        if (failed) break;
+        double* out = part_i + (size_t)(cta + L.bbase + a) * 3 * IB + w * 32 * P + lane;
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            out[0 * IB + k * 32] = tx[k];
+            out[1 * IB + k * 32] = ty[k];
+            out[2 * IB + k * 32] = tz[k];
+        }
+    }
+    if (failed) {
+        if (threadIdx.x == 0) atomicOr(err_word, NB_DEVERR_TIMEOUT);
+        for (uint32_t k = iter; k < iter + 2 && u0 + k < u1; ++k)
+            mbar_wait(&full[k & 1], (k >> 1) & 1);
+    }
+}
+
 // Per body: its i-side partials (CTA order) and the j-side partials of the units above the
 // diagonal in its column (I-block order), summed in FP64 and, for the FP64 form (whose masses are
 // not scaled), multiplied by G.
@@ -393,26 +609,37 @@ namespace nb {
     X(0, 8, 12, 128) X(1, 4, 12, 256) X(2, 4, 12, 128) X(3, 4, 16, 128) X(4, 8, 8, 256)       \
         X(5, 4, 8, 256) X(6, 8, 6, 256) X(7, 2, 12, 128)
 #define NB_SYM64_CONFIG_LIST(X) X(0, 4, 2, 64) X(1, 4, 4, 64) X(2, 8, 2, 64) X(3, 4, 2, 128)
+#define NB_SYMDF_CONFIG_LIST(X) X(0, 4, 2, 64) X(1, 4, 4, 64)
 
 #define NB_SYM_ROW(i, W, P, JT) {W, P, JT},
 const SymConfig kSymConfigs[NB_SYM_CONFIGS] = {NB_SYM_CONFIG_LIST(NB_SYM_ROW)};
 const SymConfig kSym64Configs[NB_SYM64_CONFIGS] = {NB_SYM64_CONFIG_LIST(NB_SYM_ROW)};
+const SymConfig kSymDfConfigs[NB_SYMDF_CONFIGS] = {NB_SYMDF_CONFIG_LIST(NB_SYM_ROW)};
 #undef NB_SYM_ROW
 
 namespace {
 
-int g_sym_ctas_per_sm[NB_SYM_CONFIGS] = {};
-int g_sym64_ctas_per_sm[NB_SYM64_CONFIGS] = {};
+int g_sym_ctas_per_sm[3][NB_SYM_CONFIGS] = {};
+
+template <typename K>
+nb_status occupancy(K kernel, int threads, size_t smem, int* out) {
+    NB_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    NB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kernel, threads, smem));
+    if (*out < 1) *out = 1;
+    return NB_OK;
+}
 
 template <typename R, int W, int P, int JT>
 nb_status sym_prepare(int* out) {
-    constexpr size_t smem = nbsym::sym_smem_bytes<R, W, P, JT>();
-    NB_CUDA_TRY(cudaFuncSetAttribute(nbsym::pair_sym_kernel<R, W, P, JT>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    NB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        out, nbsym::pair_sym_kernel<R, W, P, JT>, 32 * W, smem));
-    if (*out < 1) *out = 1;
-    return NB_OK;
+    return occupancy(nbsym::pair_sym_kernel<R, W, P, JT>, 32 * W,
+                     nbsym::sym_smem_bytes<R, W, P, JT>(), out);
+}
+
+template <int W, int P, int JT>
+nb_status sym_df_prepare(int* out) {
+    return occupancy(nbsym::pair_sym_df_kernel<W, P, JT>, 32 * W,
+                     nbsym::sym_df_smem_bytes<W, P, JT>(), out);
 }
 
 template <typename R, int W, int P, int JT>
@@ -429,30 +656,62 @@ nb_status sym_launch_cfg(const nbsym::SymPlan& S, const void* src, double eps2, 
     return check_launch("sym_combine_kernel");
 }
 
-const SymConfig& config_of(bool f64, int cfg) {
-    return f64 ? kSym64Configs[cfg] : kSymConfigs[cfg];
+template <int W, int P, int JT>
+nb_status sym_df_launch_cfg(const nbsym::SymPlan& S, const void* src, double eps2, void* part_i,
+                            void* part_j, double* ax, double* ay, double* az, uint32_t* err_word,
+                            cudaStream_t stream) {
+    const float e2h = (float)eps2, e2l = (float)(eps2 - (double)e2h);
+    nbsym::pair_sym_df_kernel<W, P, JT>
+        <<<S.ctas, 32 * W, nbsym::sym_df_smem_bytes<W, P, JT>(), stream>>>(
+            S, (const nbsym::RecTF*)src, e2h, e2l, (double*)part_i, (double*)part_j, err_word);
+    NB_TRY(check_launch("pair_sym_df_kernel"));
+    // G is folded into the double-float masses: the combine scales by 1
+    nbsym::sym_combine_kernel<double, 32 * W * P, JT>
+        <<<ceil_div(S.n_total, 256), 256, 0, stream>>>(S, (const double*)part_i,
+                                                       (const double*)part_j, 1.0, ax, ay, az);
+    return check_launch("sym_combine_kernel");
+}
+
+const SymConfig& config_of(int form, int cfg) {
+    return form == SYM_F64 ? kSym64Configs[cfg]
+                           : (form == SYM_DF ? kSymDfConfigs[cfg] : kSymConfigs[cfg]);
 }
 
 }  // namespace
 
-uint32_t sym_ib(bool f64, int cfg) {
-    const SymConfig& C = config_of(f64, cfg);
+int sym_config_count(int form) {
+    return form == SYM_F64 ? NB_SYM64_CONFIGS
+                           : (form == SYM_DF ? NB_SYMDF_CONFIGS : NB_SYM_CONFIGS);
+}
+
+uint32_t sym_ib(int form, int cfg) {
+    const SymConfig& C = config_of(form, cfg);
     return 32u * C.warps * C.p;
 }
 
-size_t sym_record_bytes(bool f64) { return f64 ? sizeof(nbsym::Rec64) : sizeof(float4); }
+size_t sym_record_bytes(int form) {
+    return form == SYM_F64 ? sizeof(nbsym::Rec64)
+                           : (form == SYM_DF ? sizeof(nbsym::RecTF) : sizeof(float4));
+}
 
-nb_status sym_ctas_per_sm(bool f64, int cfg, int* out) {
-    if (cfg < 0 || cfg >= (f64 ? NB_SYM64_CONFIGS : NB_SYM_CONFIGS))
-        return set_error(NB_ERR_INVALID_ARG, "bad symmetric pair config %d", cfg);
-    int* cache = f64 ? g_sym64_ctas_per_sm : g_sym_ctas_per_sm;
-    if (cache[cfg] == 0) {
+nb_status sym_ctas_per_sm(int form, int cfg, int* out) {
+    if (form < SYM_F32 || form > SYM_DF || cfg < 0 || cfg >= sym_config_count(form))
+        return set_error(NB_ERR_INVALID_ARG, "bad symmetric pair config %d/%d", form, cfg);
+    int& cached = g_sym_ctas_per_sm[form][cfg];
+    if (cached == 0) {
         int v = 0;
-        if (f64) {
+        if (form == SYM_F64) {
             switch (cfg) {
 #define NB_SYM_PREP(i, W, P, JT) \
     case i: NB_TRY((sym_prepare<double, W, P, JT>(&v))); break;
                 NB_SYM64_CONFIG_LIST(NB_SYM_PREP)
+#undef NB_SYM_PREP
+            }
+        } else if (form == SYM_DF) {
+            switch (cfg) {
+#define NB_SYM_PREP(i, W, P, JT) \
+    case i: NB_TRY((sym_df_prepare<W, P, JT>(&v))); break;
+                NB_SYMDF_CONFIG_LIST(NB_SYM_PREP)
 #undef NB_SYM_PREP
             }
         } else {
@@ -463,18 +722,18 @@ nb_status sym_ctas_per_sm(bool f64, int cfg, int* out) {
 #undef NB_SYM_PREP
             }
         }
-        cache[cfg] = v;
+        cached = v;
     }
-    *out = cache[cfg];
+    *out = cached;
     return NB_OK;
 }
 
-nb_status sym_host_plan(bool f64, int cfg, const uint32_t* counts, uint32_t n_systems,
+nb_status sym_host_plan(int form, int cfg, const uint32_t* counts, uint32_t n_systems,
                         int sm_count, SymHostPlan* out) {
     int per_sm = 0;
-    NB_TRY(sym_ctas_per_sm(f64, cfg, &per_sm));
-    const SymConfig& C = config_of(f64, cfg);
-    const uint32_t ib = sym_ib(f64, cfg), tpb = ib / (uint32_t)C.jt;
+    NB_TRY(sym_ctas_per_sm(form, cfg, &per_sm));
+    const SymConfig& C = config_of(form, cfg);
+    const uint32_t ib = sym_ib(form, cfg), tpb = ib / (uint32_t)C.jt;
     out->sys.assign(n_systems + 1, nbsym::SymSys{0, 0, 0, 0, 0});
     for (uint32_t s = 0; s < n_systems; ++s) {
         const nbsym::SymSys& A = out->sys[s];
@@ -497,12 +756,12 @@ nb_status sym_host_plan(bool f64, int cfg, const uint32_t* counts, uint32_t n_sy
     return NB_OK;
 }
 
-size_t sym_part_i_bytes(bool f64, int cfg, uint32_t ctas, uint32_t n_blocks) {
-    // FP32: (hi, lo) per axis; FP64: one value per axis
-    return ((size_t)ctas + n_blocks) * sym_ib(f64, cfg) * (f64 ? 3 * 8 : 6 * 4);
+size_t sym_part_i_bytes(int form, int cfg, uint32_t ctas, uint32_t n_blocks) {
+    // FP32: (hi, lo) per axis; FP64 and double-float: one FP64 value per axis
+    return ((size_t)ctas + n_blocks) * sym_ib(form, cfg) * (form == SYM_F32 ? 6 * 4 : 3 * 8);
 }
-size_t sym_part_j_bytes(bool f64, int cfg, uint64_t units) {
-    return (size_t)units * 3 * config_of(f64, cfg).jt * (f64 ? 8 : 4);
+size_t sym_part_j_bytes(int form, int cfg, uint64_t units) {
+    return (size_t)units * 3 * config_of(form, cfg).jt * (form == SYM_F32 ? 4 : 8);
 }
 
 nb_status sym_single_table(nbsym::SymSys* sys, const SymHostPlan& hp, cudaStream_t stream) {
@@ -511,28 +770,41 @@ nb_status sym_single_table(nbsym::SymSys* sys, const SymHostPlan& hp, cudaStream
     return check_launch("sym_single_table_kernel");
 }
 
-nb_status sym_launch(bool f64, int cfg, const nbsym::SymPlan& S, const double* m, const double* x,
+nb_status sym_launch(int form, int cfg, const nbsym::SymPlan& S, const double* m, const double* x,
                      const double* y, const double* z, double G, double eps2, void* src,
                      void* part_i, void* part_j, double* ax, double* ay, double* az,
                      uint32_t* err_word, cudaStream_t stream) {
     int per_sm = 0;
-    NB_TRY(sym_ctas_per_sm(f64, cfg, &per_sm));  // shared-memory opt-in before the first launch
+    NB_TRY(sym_ctas_per_sm(form, cfg, &per_sm));  // shared-memory opt-in before the first launch
     if (S.units == 0) return NB_OK;
-    if (f64) {
-        nbsym::sym_prepare_kernel<double><<<ceil_div(S.n_records, 256), 256, 0, stream>>>(
-            S, m, x, y, z, G, (nbsym::Rec64*)src);
+    const int blocks = ceil_div(S.n_records, 256);
+    if (form == SYM_F64) {
+        nbsym::sym_prepare_kernel<double><<<blocks, 256, 0, stream>>>(S, m, x, y, z, G,
+                                                                      (nbsym::Rec64*)src);
+    } else if (form == SYM_DF) {
+        nbsym::sym_prepare_tf_kernel<<<blocks, 256, 0, stream>>>(S, m, x, y, z, G,
+                                                                 (nbsym::RecTF*)src);
     } else {
-        nbsym::sym_prepare_kernel<float><<<ceil_div(S.n_records, 256), 256, 0, stream>>>(
-            S, m, x, y, z, G, (float4*)src);
+        nbsym::sym_prepare_kernel<float><<<blocks, 256, 0, stream>>>(S, m, x, y, z, G,
+                                                                     (float4*)src);
     }
     NB_TRY(check_launch("sym_prepare_kernel"));
-    if (f64) {
+    if (form == SYM_F64) {
         switch (cfg) {
 #define NB_SYM_LAUNCH(i, W, P, JT)                                                          \
     case i:                                                                                 \
         return sym_launch_cfg<double, W, P, JT>(S, src, eps2, part_i, part_j, G, ax, ay, az, \
                                                 err_word, stream);
             NB_SYM64_CONFIG_LIST(NB_SYM_LAUNCH)
+#undef NB_SYM_LAUNCH
+        }
+    } else if (form == SYM_DF) {
+        switch (cfg) {
+#define NB_SYM_LAUNCH(i, W, P, JT)                                                         \
+    case i:                                                                                \
+        return sym_df_launch_cfg<W, P, JT>(S, src, eps2, part_i, part_j, ax, ay, az, err_word, \
+                                           stream);
+            NB_SYMDF_CONFIG_LIST(NB_SYM_LAUNCH)
 #undef NB_SYM_LAUNCH
         }
     } else {
@@ -545,7 +817,7 @@ nb_status sym_launch(bool f64, int cfg, const nbsym::SymPlan& S, const double* m
 #undef NB_SYM_LAUNCH
         }
     }
-    return set_error(NB_ERR_INVALID_ARG, "bad symmetric pair config %d", cfg);
+    return set_error(NB_ERR_INVALID_ARG, "bad symmetric pair config %d/%d", form, cfg);
 }
 
 }  // namespace nb

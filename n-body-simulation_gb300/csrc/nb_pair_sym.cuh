@@ -1,5 +1,5 @@
-// nb_pair_sym.cuh -- plan and launcher of the symmetric pair kernel (nb_pair_sym.cu), FP32 with
-// compensated accumulation or FP64.
+// nb_pair_sym.cuh -- plan and launcher of the symmetric pair kernel (nb_pair_sym.cu): FP32 with
+// compensated accumulation, FP64, or double-float.
 #pragma once
 #include <vector>
 
@@ -33,21 +33,28 @@ __host__ __device__ __forceinline__ uint64_t row_off(uint32_t n_jt, uint32_t tpb
 
 namespace nb {
 
+// Arithmetic form of the symmetric kernel: FP32 with compensated sums, FP64, or double-float
+// (FP64-accurate pair arithmetic on the FP32 pipe).
+enum SymForm : int { SYM_F32 = 0, SYM_F64 = 1, SYM_DF = 2 };
+
 // Tile shape: warps per CTA, bodies per lane, j-tile bodies.
 struct SymConfig {
     int warps, p, jt;
 };
 constexpr int NB_SYM_CONFIGS = 8;    // FP32 shapes
 constexpr int NB_SYM64_CONFIGS = 4;  // FP64 shapes
+constexpr int NB_SYMDF_CONFIGS = 2;  // double-float shapes
 extern const SymConfig kSymConfigs[NB_SYM_CONFIGS];
 extern const SymConfig kSym64Configs[NB_SYM64_CONFIGS];
+extern const SymConfig kSymDfConfigs[NB_SYMDF_CONFIGS];
+int sym_config_count(int form);
 
-// Bodies per I-block of a shape, and bytes per source record (16 FP32, 32 FP64).
-uint32_t sym_ib(bool f64, int cfg);
-size_t sym_record_bytes(bool f64);
+// Bodies per I-block of a shape, and bytes per source record (16 FP32, 32 FP64, 48 double-float).
+uint32_t sym_ib(int form, int cfg);
+size_t sym_record_bytes(int form);
 
 // Resident CTAs per SM of a shape (also opts it into its dynamic shared memory).
-nb_status sym_ctas_per_sm(bool f64, int cfg, int* out);
+nb_status sym_ctas_per_sm(int form, int cfg, int* out);
 
 // Host side of a plan: the per-system table and the totals.
 struct SymHostPlan {
@@ -55,16 +62,16 @@ struct SymHostPlan {
     uint64_t units = 0;
     uint32_t n_total = 0, n_records = 0, n_blocks = 0, ctas = 0;
 };
-nb_status sym_host_plan(bool f64, int cfg, const uint32_t* counts, uint32_t n_systems,
+nb_status sym_host_plan(int form, int cfg, const uint32_t* counts, uint32_t n_systems,
                         int sm_count, SymHostPlan* out);
 // Scratch of a plan: i-side and j-side partials (bytes); records take
-// n_records * sym_record_bytes(f64).
-size_t sym_part_i_bytes(bool f64, int cfg, uint32_t ctas, uint32_t n_blocks);
-size_t sym_part_j_bytes(bool f64, int cfg, uint64_t units);
+// n_records * sym_record_bytes(form).
+size_t sym_part_i_bytes(int form, int cfg, uint32_t ctas, uint32_t n_blocks);
+size_t sym_part_j_bytes(int form, int cfg, uint64_t units);
 // Writes the device table of a single-system plan (two entries) with a kernel.
 nb_status sym_single_table(nbsym::SymSys* sys, const SymHostPlan& hp, cudaStream_t stream);
 // Launches prepare + symmetric pair kernel + combine for a plan whose device table is filled.
-nb_status sym_launch(bool f64, int cfg, const nbsym::SymPlan& S, const double* m, const double* x,
+nb_status sym_launch(int form, int cfg, const nbsym::SymPlan& S, const double* m, const double* x,
                      const double* y, const double* z, double G, double eps2, void* src,
                      void* part_i, void* part_j, double* ax, double* ay, double* az,
                      uint32_t* err_word, cudaStream_t stream);

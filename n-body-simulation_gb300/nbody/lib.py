@@ -201,7 +201,7 @@ SIGNATURES.update({
     "nb_util_fma_peak": [_vp, _i, C.POINTER(_d)],
     "nb_bh_set_schedule": [_i],
     "nb_naive_set_pair_config": [_i],
-    "nb_naive_set_symmetric": [_i, _i, _i],
+    "nb_naive_set_symmetric": [_i, _i, _i, _i],
     "nb_batch_create": [_vp, _u32, _vp, C.POINTER(_vp)],
     "nb_batch_destroy": [_vp],
     "nb_batch_info": [_vp, C.POINTER(_u32), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i),
@@ -410,10 +410,11 @@ def set_naive_pair_config(config: int):
 SYM_NEVER, SYM_AUTO, SYM_ALWAYS = 0, 1, 2
 
 
-def set_naive_symmetric(mode: int = SYM_AUTO, config: int = 0, config_f64: int = 0):
-    """Selection of the symmetric pair kernel for full-range NB_F32C / NB_F64 evaluations and
-    its FP32 and FP64 tile shapes."""
-    check(load().nb_naive_set_symmetric(mode, config, config_f64))
+def set_naive_symmetric(mode: int = SYM_AUTO, config: int = 0, config_f64: int = 0,
+                        config_df: int = 0):
+    """Selection of the symmetric pair kernel for full-range NB_F32C / NB_F64 / NB_DF64
+    evaluations and its FP32, FP64 and double-float tile shapes."""
+    check(load().nb_naive_set_symmetric(mode, config, config_f64, config_df))
 
 
 class Batch:

@@ -4,7 +4,8 @@ NaiveAlgorithm.cpp:262-360, through the C ABI.
 
 Tolerances (those of the one-sided kernels): NB_F32C per-body relative error median <= 1e-5 and
 max <= 1e-3 on Plummer spheres (eps = 1e-3), median <= 1e-4 on the heliocentric disc; NB_F64
-per-body relative error <= 1e-12; repeated calls bit-identical (fixed combine order).
+per-body relative error <= 1e-12; NB_DF64 median relative error <= 1e-12 and per-body error
+<= 1e-11 of max(|a|, median |a|); repeated calls bit-identical (fixed combine order).
 """
 
 import numpy as np
@@ -26,18 +27,18 @@ def ctx():
     c.close()
 
 
-def run_f32c(ctx, d, eps2, mode, config=0, precision="f32c", config_f64=0):
+def run_f32c(ctx, d, eps2, mode, config=0, precision="f32c", config_f64=0, config_df=0):
     import torch
     from nbody.lib import SYM_AUTO, set_naive_symmetric
     t = {k: dev(d[k]) for k in ("m", "x", "y", "z")}
     n = len(d["m"])
     a = [torch.full((n,), float("nan"), dtype=torch.float64, device="cuda") for _ in range(3)]
     try:
-        set_naive_symmetric(mode, config, config_f64)
+        set_naive_symmetric(mode, config, config_f64, config_df)
         ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *a, d["G"], eps2, precision)
         ctx.sync()
     finally:
-        set_naive_symmetric(SYM_AUTO, 0, 0)
+        set_naive_symmetric(SYM_AUTO, 0, 0, 0)
     return tuple(host(v) for v in a)
 
 
@@ -126,3 +127,39 @@ def test_symmetric_f64_deterministic_and_selected(ctx):
     for a, f in zip(auto, forced):
         np.testing.assert_array_equal(a, f)
     assert rel_err(*auto, *one).max() <= 2e-12
+
+
+@pytest.mark.parametrize("config_df", [0, 1])
+@pytest.mark.parametrize("kind,n,eps2", [("disc", 16384, 1e-22), ("plummer", 5000, 1e-6),
+                                         ("disc", 1, 1e-22), ("plummer", 129, 1e-6)])
+def test_symmetric_df64_fp64_accurate(ctx, kind, n, eps2, config_df):
+    """The double-float form against the FP64 oracle with the one-sided double-float bounds."""
+    from nbody.lib import SYM_ALWAYS
+    if config_df and n != 5000:
+        pytest.skip("other sizes run with the default double-float shape only")
+    d = bodies(kind, n, seed=4)
+    got = run_f32c(ctx, d, eps2, SYM_ALWAYS, precision="df64", config_df=config_df)
+    if n == 1:
+        assert all(np.all(g == 0) for g in got)
+        return
+    ref = oracle.naive_accel(d["m"], d["x"], d["y"], d["z"], d["G"], eps2)
+    diff = np.sqrt(sum((g - r) ** 2 for g, r in zip(got, ref)))
+    mag = np.sqrt(sum(r * r for r in ref))
+    assert np.median(rel_err(*got, *ref)) <= 1e-12
+    assert (diff / np.maximum(mag, np.median(mag))).max() <= 1e-11
+
+
+def test_symmetric_df64_selected_and_deterministic(ctx):
+    """At 16,384 bodies the automatic mode takes the double-float symmetric kernel; repeated
+    calls agree bit for bit and differ from the one-sided double-float kernel by rounding only."""
+    from nbody.lib import SYM_AUTO, SYM_NEVER
+    d = bodies("disc", 16384, seed=6)
+    first = run_f32c(ctx, d, 1e-22, SYM_AUTO, precision="df64")
+    second = run_f32c(ctx, d, 1e-22, SYM_AUTO, precision="df64")
+    one = run_f32c(ctx, d, 1e-22, SYM_NEVER, precision="df64")
+    for f, s in zip(first, second):
+        np.testing.assert_array_equal(f, s)
+    mag = np.sqrt(sum(r * r for r in one))
+    diff = np.sqrt(sum((f - o) ** 2 for f, o in zip(first, one)))
+    assert (diff / np.maximum(mag, np.median(mag))).max() <= 1e-11
+    assert any(np.any(f != o) for f, o in zip(first, one))  # a different kernel ran
