@@ -36,10 +36,10 @@ THETA = 0.5
 DT = 1.0 / 24
 EPS2 = 1e-22
 SEED = 1
-# kernels of ours launched per step: kick_drift 1, build 51 (aabb 1, keys 1, radix 8 x (hist 1 +
-# scan 3 + scatter 1), runs 1, splits 1, count 1, scan 3, emit 1, centre of mass 1, records 1),
-# traversal 1, kick 1
-LAUNCHES_PER_STEP = 54
+# kernels of ours launched per step: kick_drift 1, build 21 (aabb 1, keys 1, radix 10 (one
+# histogram of all digits, their offsets, 8 look-back passes), runs 1, splits 1, count 1, scan 3,
+# emit 1, centre of mass 1, records 1), traversal 1, kick 1
+LAUNCHES_PER_STEP = 24
 # algorithmic FLOP of the traversal (Nyland's 20 per pair interaction for an accepted cell; an
 # opened cell costs its distance test: 3 sub, 3 mul, 2 add, 1 rsqrt, 1 mul = 10)
 FLOP_ACCEPTED, FLOP_OPENED = 20, 10
@@ -320,7 +320,7 @@ def run_ours(args):
     phase_bytes = {
         "aabb": 24 * n,                                  # read x, y, z
         "keys": 24 * n + 12 * n,                         # read x, y, z; write key + id
-        "sort": 8 * 24 * n,                              # 8 radix passes: read + write key + id
+        "sort": 8 * 24 * n + 8 * n,                      # 8 passes: read + write key + id; histogram
         "cells": 16 * n + 29 * n + 12 * n + 8 * n + 24 * nodes,  # runs, splits, counts, scan,
                                                          # emit (node level/first/last/skip/...)
         "centre_of_mass": 64 * n + 305 * nodes,          # body sums + sorted records; per node:

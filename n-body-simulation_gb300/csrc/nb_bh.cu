@@ -18,6 +18,8 @@
 //     octant order 0..7 (bit-identical to BarnesHutOctree.cpp:304-311).
 #include <cuda/atomic>
 
+#include <algorithm>
+
 #include "nb_bh.cuh"
 #include "nb_sort.cuh"
 
@@ -38,32 +40,44 @@ __device__ __forceinline__ uint64_t ordered_bits(double v) {
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
-// Octant digits of levels [word*21, word*21+21) for a body: the reference's FP64 recurrence
+// Inverse of ordered_bits.
+__device__ __forceinline__ double from_ordered(uint64_t o) {
+    return __longlong_as_double((long long)((o >> 63) ? (o & ~0x8000000000000000ull) : ~o));
+}
+
+// The edge halvings of the recurrence: exponent decrements while they stay exact (the normal,
+// positive edges of <= 42 levels), otherwise (a zero or tiny box) FP64 divisions by 2.
+struct Halving {
+    double e;
+    uint64_t e_bits;
+    bool bits;
+    __device__ explicit Halving(double edge) : e(edge) {
+        e_bits = (uint64_t)__double_as_longlong(edge);
+        bits = (e_bits >> 52) > 64 && (e_bits >> 52) < 0x7ff;
+    }
+    // edge / 2 of the next level
+    __device__ double next() {
+        if (bits) {
+            e_bits -= 1ull << 52;
+            return __longlong_as_double((long long)e_bits);
+        }
+        e = e / 2;
+        return e;
+    }
+};
+
+// Octant digits of levels [L0, last) appended to `key` for a body (ordered bits ox, oy, oz of
+// its coordinates), from the cell mins entering level L0: the reference's FP64 recurrence
 // (mid = min + edge/2 rounded as FP64, strict compares, child min = mid or min). Only the three
 // midpoint additions per level run on the FP64 pipe: the compares are integer compares of
 // order-preserving bit patterns (exact: a midpoint is never -0 since edge/2 > 0, and the body's
-// -0 coordinates are taken as +0, which compares equal), and edge/2 is an exponent decrement
-// (exact for the normal, positive edges of <= 42 levels).
-__device__ uint64_t key_word(const double* __restrict__ box, double px, double py, double pz,
-                             int word) {
-    double mnx = box[0], mny = box[1], mnz = box[2], e = box[6];
-    uint64_t e_bits = (uint64_t)__double_as_longlong(e);
-    // exponent decrements stay exact while the edge is positive and normal after 42 halvings;
-    // otherwise (a zero or tiny box) the halving is an FP64 multiply
-    const bool halve_bits = (e_bits >> 52) > 64 && (e_bits >> 52) < 0x7ff;
-    const uint64_t ox = ordered_bits(px == 0.0 ? 0.0 : px), oy = ordered_bits(py == 0.0 ? 0.0 : py),
-                   oz = ordered_bits(pz == 0.0 ? 0.0 : pz);
-    uint64_t key = 0;
-    const int first = word * NB_KEY_LEVELS, last = first + NB_KEY_LEVELS;
-    for (int L = 0; L < last; ++L) {
-        double ce;
-        if (halve_bits) {
-            e_bits -= 1ull << 52;  // edge / 2
-            ce = __longlong_as_double((long long)e_bits);
-        } else {
-            ce = e / 2;
-            e = ce;
-        }
+// -0 coordinates are taken as +0, which compares equal). Digits of levels below `first` are not
+// appended.
+__device__ uint64_t key_levels(Halving h, uint64_t ox, uint64_t oy, uint64_t oz, double mnx,
+                               double mny, double mnz, int L0, int first, int last,
+                               uint64_t key) {
+    for (int L = L0; L < last; ++L) {
+        const double ce = h.next();
         const double midx = __dadd_rn(mnx, ce);
         const double midy = __dadd_rn(mny, ce);
         const double midz = __dadd_rn(mnz, ce);
@@ -79,14 +93,78 @@ __device__ uint64_t key_word(const double* __restrict__ box, double px, double p
     return key;
 }
 
-__global__ void keys_kernel(const double* __restrict__ x, const double* __restrict__ y,
-                            const double* __restrict__ z, uint32_t n,
-                            const double* __restrict__ box, uint64_t* __restrict__ key0,
-                            uint32_t* __restrict__ ids) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    key0[i] = key_word(box, x[i], y[i], z[i], 0);
-    ids[i] = i;
+__device__ __forceinline__ uint64_t ordered_coord(double v) {
+    return ordered_bits(v == 0.0 ? 0.0 : v);
+}
+
+// Octant digits of levels [word*21, word*21+21) for a body, from the root.
+__device__ uint64_t key_word(const double* __restrict__ box, double px, double py, double pz,
+                             int word) {
+    const int first = word * NB_KEY_LEVELS;
+    return key_levels(Halving(box[6]), ordered_coord(px), ordered_coord(py), ordered_coord(pz),
+                      box[0], box[1], box[2], 0, first, first + NB_KEY_LEVELS, 0);
+}
+
+// Levels resolved through the per-block midpoint table of keys_kernel.
+constexpr int KT_LEVELS = 10;
+constexpr int KT_ENTRIES = (1 << KT_LEVELS) - 1;
+
+// First key word of every body. The top KT_LEVELS levels of each axis have at most 2^L distinct
+// cells per level, so each block first evaluates the reference's FP64 midpoints of those cells
+// once (mids[axis][2^L - 1 + prefix], prefix = the path's upper/lower bits of levels < L, with the
+// same recurrence and halvings) and the bodies then walk those levels with integer compares
+// against the table; the FP64 recurrence resumes at level KT_LEVELS from the table's mins. The
+// digits are those of key_word, bit for bit.
+__global__ void __launch_bounds__(BH_THREADS)
+keys_kernel(const double* __restrict__ x, const double* __restrict__ y,
+            const double* __restrict__ z, uint32_t n, const double* __restrict__ box,
+            uint64_t* __restrict__ key0, uint32_t* __restrict__ ids) {
+    __shared__ uint64_t mids[3][KT_ENTRIES];
+    {
+        Halving h(box[6]);
+        for (int L = 0; L < KT_LEVELS; ++L) {
+            const double ce = h.next();
+            for (int t = threadIdx.x; t < (1 << L); t += blockDim.x) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    double mn = box[a];
+                    for (int l = 0; l < L; ++l)  // upper half at level l: min = that midpoint
+                        if ((t >> (L - 1 - l)) & 1)
+                            mn = from_ordered(mids[a][(1 << l) - 1 + (t >> (L - l))]);
+                    mids[a][(1 << L) - 1 + t] = ordered_bits(__dadd_rn(mn, ce));
+                }
+            }
+            __syncthreads();
+        }
+    }
+    Halving h0(box[6]);
+    for (int l = 0; l < KT_LEVELS; ++l) h0.next();  // the edge entering level KT_LEVELS
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t ox = ordered_coord(x[i]), oy = ordered_coord(y[i]),
+                       oz = ordered_coord(z[i]);
+        uint64_t key = 0;
+        uint32_t tx = 0, ty = 0, tz = 0;  // paths so far (1 = upper half)
+        uint64_t ux = 0, uy = 0, uz = 0;  // last upper midpoints (ordered bits), 0 = none
+#pragma unroll
+        for (int L = 0; L < KT_LEVELS; ++L) {
+            const int base = (1 << L) - 1;
+            const uint64_t mx = mids[0][base + tx], my = mids[1][base + ty],
+                           mz = mids[2][base + tz];
+            const bool up = oy > my, rt = ox > mx, bk = oz < mz;
+            key = (key << 3) |
+                  nb_visit_of_octant((uint32_t)up * 4u + (uint32_t)rt * 2u + (uint32_t)bk);
+            tx = 2 * tx + rt;
+            ty = 2 * ty + up;
+            tz = 2 * tz + !bk;
+            if (rt) ux = mx;
+            if (up) uy = my;
+            if (!bk) uz = mz;
+        }
+        const double mnx = ux ? from_ordered(ux) : box[0], mny = uy ? from_ordered(uy) : box[1],
+                     mnz = uz ? from_ordered(uz) : box[2];
+        key0[i] = key_levels(h0, ox, oy, oz, mnx, mny, mnz, KT_LEVELS, 0, NB_KEY_LEVELS, key);
+        ids[i] = i;
+    }
 }
 
 // Runs of equal first words: compute the second word and insertion-sort the run (stable).
@@ -598,12 +676,14 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     NB_TRY(mark(0));
     NB_TRY(nb::launch_aabb(ctx, x, y, z, n, t->box, s));
     NB_TRY(mark(1));
-    keys_kernel<<<grid, BH_THREADS, 0, s>>>(x, y, z, n, t->box, t->key0, t->ids);
+    // persistent blocks: each evaluates the midpoint table once, then walks its bodies
+    keys_kernel<<<std::min(grid, 8 * ctx->sm_count), BH_THREADS, 0, s>>>(x, y, z, n, t->box,
+                                                                        t->key0, t->ids);
     NB_TRY(nb::check_launch("keys_kernel"));
     NB_TRY(mark(2));
     int in_alt = 0;
     NB_TRY(nb::radix_sort_pairs(t->key0, t->ids, t->key_alt, t->ids_alt, n, 0, 3 * NB_KEY_LEVELS,
-                                t->sort_temp, s, &in_alt));
+                                t->sort_temp, ctx->dev_error, s, &in_alt));
     if (in_alt) {  // an odd number of passes leaves the result in the alternate buffers
         NB_CUDA_TRY(cudaMemcpyAsync(t->key0, t->key_alt, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
         NB_CUDA_TRY(cudaMemcpyAsync(t->ids, t->ids_alt, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));

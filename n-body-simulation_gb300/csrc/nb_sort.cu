@@ -1,5 +1,7 @@
 // nb_sort.cu -- device-wide exclusive scan (u32) and stable LSD radix sort of (u64 key, u32 value)
 // pairs, used by the octree build. Deterministic: no result depends on thread timing.
+#include <algorithm>
+
 #include "nb_sort.cuh"
 
 namespace {
@@ -93,40 +95,86 @@ scan_apply_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, u
 }
 
 // ---------------------------------------------------------------------------------------------
-// Radix sort: 8-bit digits, tiles of 2048 keys (256 threads x 8 items).
+// Radix sort: 8-bit digits, tiles of 2048 keys (256 threads x 8 items), one launch per digit
+// pass. The digit histograms of all passes come from one read of the keys up front; within a
+// pass each tile finds the keys of its digit in earlier tiles by decoupled look-back (Merrill and
+// Garland, "Single-pass parallel prefix scan with decoupled look-back", NVIDIA TR 2016; the
+// radix-sort use as in Adinets and Merrill, "Onesweep", 2022): a tile publishes its per-digit
+// count, then the running total up to and including it, and reads its predecessors' words until
+// it meets a total. Tiles take their position from an atomic ticket in the order they start, so
+// a tile only waits for tiles that are already running; every wait is bounded (on timeout the
+// error word gets the timeout bit and the pass goes on). Deterministic and stable: the offsets
+// depend on the counts only.
 // ---------------------------------------------------------------------------------------------
 constexpr int RS_THREADS = 256;
 constexpr int RS_ITEMS = 8;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_BINS = 256;
+constexpr int RS_MAX_PASSES = 8;
+// look-back words: 2 flag bits over a 30-bit count (tile counts <= 2048, totals <= n < 2^30)
+constexpr uint32_t LB_AGGREGATE = 1u << 30;
+constexpr uint32_t LB_TOTAL = 2u << 30;
+constexpr uint32_t LB_VALUE = (1u << 30) - 1u;
+constexpr unsigned long long LB_WAIT_LIMIT = 1ull << 22;
 
+// hist[p][d]: keys whose digit of pass p is d, for all passes in one read.
 __global__ void __launch_bounds__(RS_THREADS)
-radix_hist_kernel(const uint64_t* __restrict__ keys, uint32_t n, int shift,
-                  uint32_t* __restrict__ hist, uint32_t n_tiles) {
-    __shared__ uint32_t h[RS_BINS];
-    h[threadIdx.x] = 0;
+radix_hist_all_kernel(const uint64_t* __restrict__ keys, uint32_t n, int begin_bit, int passes,
+                      uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[RS_MAX_PASSES][RS_BINS];
+    for (int e = threadIdx.x; e < RS_MAX_PASSES * RS_BINS; e += RS_THREADS) (&h[0][0])[e] = 0;
     __syncthreads();
-    const uint32_t base = blockIdx.x * RS_TILE;
-#pragma unroll
-    for (int k = 0; k < RS_ITEMS; ++k) {
-        const uint32_t i = base + k * RS_THREADS + threadIdx.x;
-        if (i < n) atomicAdd(&h[(uint32_t)(keys[i] >> shift) & 0xffu], 1u);
+    for (uint32_t i = blockIdx.x * RS_THREADS + threadIdx.x; i < n; i += gridDim.x * RS_THREADS) {
+        const uint64_t k = keys[i] >> begin_bit;
+        for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(uint32_t)(k >> (8 * p)) & 0xffu], 1u);
     }
     __syncthreads();
-    hist[threadIdx.x * n_tiles + blockIdx.x] = h[threadIdx.x];  // digit-major
+    for (int e = threadIdx.x; e < passes * RS_BINS; e += RS_THREADS) {
+        const uint32_t v = (&h[0][0])[e];
+        if (v) atomicAdd(&hist[e], v);
+    }
 }
 
+// hist[p][d] -> exclusive prefix over d (one block, thread d).
+__global__ void __launch_bounds__(RS_BINS) radix_offsets_kernel(uint32_t* __restrict__ hist,
+                                                                int passes) {
+    for (int p = 0; p < passes; ++p) {
+        uint32_t total;
+        const uint32_t ex = block_exclusive_scan(hist[p * RS_BINS + threadIdx.x], &total);
+        hist[p * RS_BINS + threadIdx.x] = ex;
+    }
+}
+
+__device__ __forceinline__ void lb_store(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t lb_load(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// One digit pass: keys of tile `ticket` in, ranked within the tile (warp-striped, stable),
+// placed at digit offset + keys of the digit in earlier tiles + rank.
 __global__ void __launch_bounds__(RS_THREADS)
-radix_scatter_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-                     uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
-                     int shift, const uint32_t* __restrict__ offsets, uint32_t n_tiles) {
+radix_pass_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                  uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
+                  int shift, const uint32_t* __restrict__ digit_off, uint32_t* __restrict__ lb,
+                  uint32_t* __restrict__ ticket, uint32_t* __restrict__ err) {
     __shared__ uint32_t wcnt[RS_WARPS][RS_BINS];
+    __shared__ uint32_t tile_base[RS_BINS];   // first output position of the tile's digit d
+    __shared__ uint32_t digit_local[RS_BINS];  // first tile position of digit d after the reorder
+    __shared__ uint64_t skeys[RS_TILE];
+    __shared__ uint32_t svals[RS_TILE];
+    __shared__ uint32_t tile_s;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) tile_s = atomicAdd(ticket, 1u);
     for (int b = threadIdx.x; b < RS_WARPS * RS_BINS; b += RS_THREADS) (&wcnt[0][0])[b] = 0;
     __syncthreads();
+    const uint32_t tile = tile_s;
     // warp-striped: warp w owns tile positions [w*256, w*256+256); item k, lane l -> w*256+k*32+l
-    const uint32_t base = blockIdx.x * RS_TILE + warp * (RS_ITEMS * 32);
+    const uint32_t base = tile * RS_TILE + warp * (RS_ITEMS * 32);
     uint64_t key[RS_ITEMS];
     uint32_t val[RS_ITEMS], digit[RS_ITEMS], rank[RS_ITEMS];
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -147,24 +195,63 @@ radix_scatter_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __res
         rank[k] = prev + __popc(peers & lt_mask);
     }
     __syncthreads();
-    // exclusive prefix over warps per digit; thread t owns digit t
     {
+        // thread d owns digit d: exclusive prefix over warps, the tile's count, then look-back
+        const uint32_t d = threadIdx.x;
         uint32_t run = 0;
         for (int w = 0; w < RS_WARPS; ++w) {
-            const uint32_t c = wcnt[w][threadIdx.x];
-            wcnt[w][threadIdx.x] = run;
+            const uint32_t c = wcnt[w][d];
+            wcnt[w][d] = run;
             run += c;
         }
+        uint32_t* mine = lb + (size_t)tile * RS_BINS + d;
+        uint32_t before = 0;
+        if (tile == 0) {
+            lb_store(mine, LB_TOTAL | run);
+        } else {
+            lb_store(mine, LB_AGGREGATE | run);
+            bool timed_out = false;
+            for (uint32_t t = tile; t-- > 0;) {
+                const uint32_t* w = lb + (size_t)t * RS_BINS + d;
+                uint32_t v = lb_load(w);
+                for (unsigned long long it = 0; (v & (LB_AGGREGATE | LB_TOTAL)) == 0; ++it) {
+                    if (it >= LB_WAIT_LIMIT) {
+                        timed_out = true;
+                        break;
+                    }
+                    __nanosleep(32);
+                    v = lb_load(w);
+                }
+                if (timed_out) break;
+                before += v & LB_VALUE;
+                if (v & LB_TOTAL) break;
+            }
+            if (timed_out) atomicOr(err, NB_DEVERR_TIMEOUT);
+            lb_store(mine, LB_TOTAL | (before + run));
+        }
+        tile_base[d] = digit_off[d] + before;
+        uint32_t tile_total;
+        digit_local[d] = block_exclusive_scan(run, &tile_total);  // one digit per thread
     }
     __syncthreads();
+    // reorder the tile by digit in shared memory, then write each digit's run of keys to
+    // consecutive output positions (coalesced instead of one scattered store per key)
 #pragma unroll
     for (int k = 0; k < RS_ITEMS; ++k) {
         if (digit[k] < RS_BINS) {
-            const uint32_t dst =
-                offsets[digit[k] * n_tiles + blockIdx.x] + wcnt[warp][digit[k]] + rank[k];
-            keys_out[dst] = key[k];
-            vals_out[dst] = val[k];
+            const uint32_t q = digit_local[digit[k]] + wcnt[warp][digit[k]] + rank[k];
+            skeys[q] = key[k];
+            svals[q] = val[k];
         }
+    }
+    __syncthreads();
+    const uint32_t tile_n = min((uint32_t)RS_TILE, n - tile * RS_TILE);
+    for (uint32_t q = threadIdx.x; q < tile_n; q += RS_THREADS) {
+        const uint64_t kk = skeys[q];
+        const uint32_t d = (uint32_t)(kk >> shift) & 0xffu;
+        const uint32_t dst = tile_base[d] + (q - digit_local[d]);
+        keys_out[dst] = kk;
+        vals_out[dst] = svals[q];
     }
 }
 
@@ -194,34 +281,43 @@ nb_status exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int 
     return check_launch("scan_apply_kernel");
 }
 
+// Temporary storage of radix_sort_pairs: digit offsets and tickets of all passes, then one
+// look-back word per (pass, tile, digit).
 size_t radix_temp_bytes(uint32_t n) {
-    const uint32_t tiles = (n + RS_TILE - 1) / RS_TILE;
-    const size_t hist = (size_t)tiles * RS_BINS;
-    return (2 * hist + 1) * sizeof(uint32_t) + scan_temp_bytes((uint32_t)hist) + 256;
+    const size_t tiles = (n + RS_TILE - 1) / RS_TILE;
+    return ((size_t)RS_MAX_PASSES * RS_BINS + 64 + (size_t)RS_MAX_PASSES * tiles * RS_BINS) *
+           sizeof(uint32_t);
 }
 
 nb_status radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
                            uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit,
-                           void* temp, cudaStream_t stream, int* result_in_alt) {
+                           void* temp, uint32_t* err, cudaStream_t stream, int* result_in_alt) {
     *result_in_alt = 0;
     if (n <= 1) return NB_OK;
+    const int passes = (end_bit - begin_bit + 7) / 8;
+    if (passes < 1 || passes > RS_MAX_PASSES)
+        return set_error(NB_ERR_INVALID_ARG, "radix_sort_pairs: bit range [%d, %d)", begin_bit,
+                         end_bit);
     const uint32_t tiles = (n + RS_TILE - 1) / RS_TILE;
-    const uint32_t hist_n = tiles * RS_BINS;
-    uint32_t* hist = (uint32_t*)temp;
-    uint32_t* offs = hist + hist_n;
-    uint32_t* scan_tmp = offs + hist_n + 1;
+    uint32_t* offs = (uint32_t*)temp;                   // [passes][256]
+    uint32_t* tickets = offs + RS_MAX_PASSES * RS_BINS;  // [passes]
+    uint32_t* lb = tickets + 64;                         // [passes][tiles][256]
+    NB_CUDA_TRY(cudaMemsetAsync(temp, 0, radix_temp_bytes(n), stream));
+    const int hist_blocks = (int)std::min<uint32_t>(tiles, 1024u);
+    radix_hist_all_kernel<<<hist_blocks, RS_THREADS, 0, stream>>>(keys, n, begin_bit, passes, offs);
+    NB_TRY(check_launch("radix_hist_all_kernel"));
+    radix_offsets_kernel<<<1, RS_BINS, 0, stream>>>(offs, passes);
+    NB_TRY(check_launch("radix_offsets_kernel"));
     uint64_t* kin = keys;
     uint32_t* vin = vals;
     uint64_t* kout = keys_alt;
     uint32_t* vout = vals_alt;
     int flips = 0;
-    for (int shift = begin_bit; shift < end_bit; shift += 8) {
-        radix_hist_kernel<<<tiles, RS_THREADS, 0, stream>>>(kin, n, shift, hist, tiles);
-        NB_TRY(check_launch("radix_hist_kernel"));
-        NB_TRY(exclusive_scan_u32(hist, offs, hist_n, 0, scan_tmp, stream));
-        radix_scatter_kernel<<<tiles, RS_THREADS, 0, stream>>>(kin, vin, kout, vout, n, shift, offs,
-                                                              tiles);
-        NB_TRY(check_launch("radix_scatter_kernel"));
+    for (int p = 0; p < passes; ++p) {
+        radix_pass_kernel<<<tiles, RS_THREADS, 0, stream>>>(
+            kin, vin, kout, vout, n, begin_bit + 8 * p, offs + p * RS_BINS,
+            lb + (size_t)p * tiles * RS_BINS, tickets + p, err);
+        NB_TRY(check_launch("radix_pass_kernel"));
         uint64_t* tk = kin;
         kin = kout;
         kout = tk;
@@ -254,7 +350,8 @@ nb_status nb_util_radix_sort_pairs(nb_ctx* ctx, uint64_t* keys, uint32_t* vals, 
     NB_CUDA_TRY(cudaMallocAsync(&va, (size_t)n * 4, s));
     NB_CUDA_TRY(cudaMallocAsync(&tmp, nb::radix_temp_bytes(n), s));
     int in_alt = 0;
-    nb_status st = nb::radix_sort_pairs(keys, vals, ka, va, n, begin_bit, end_bit, tmp, s, &in_alt);
+    nb_status st = nb::radix_sort_pairs(keys, vals, ka, va, n, begin_bit, end_bit, tmp,
+                                        ctx->dev_error, s, &in_alt);
     if (st == NB_OK && in_alt) {
         cudaMemcpyAsync(keys, ka, (size_t)n * 8, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(vals, va, (size_t)n * 4, cudaMemcpyDeviceToDevice, s);
