@@ -241,7 +241,7 @@ def run_ours(args):
     import torch
 
     from nbody import generators
-    from nbody.lib import BHTree, Context, fma_peak
+    from nbody.lib import REC_FP64, BHTree, Context, fma_peak
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -266,6 +266,7 @@ def run_ours(args):
     acc = [torch.zeros(n, **f64) for _ in range(3)]
     vh = [torch.zeros(n, **f64) for _ in range(3)]
     tree = BHTree(ctx, n, theta=THETA)
+    tree.set_records(REC_FP64)  # the node records the FP64 per-body rule reads
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     trav_ev = []
 
@@ -323,9 +324,11 @@ def run_ours(args):
         "sort": 8 * 24 * n + 8 * n,                      # 8 passes: read + write key + id; histogram
         "cells": 16 * n + 29 * n + 12 * n + 8 * n + 24 * nodes,  # runs, splits, counts, scan,
                                                          # emit (node level/first/last/skip/...)
-        "centre_of_mass": 64 * n + 305 * nodes,          # body sums + sorted records; per node:
-                                                         # child sums read, sums, child list and
-                                                         # traversal records written
+        "centre_of_mass": 64 * n + 192 * nodes,          # body m, x, y, z read, leaf sums
+                                                         # written; per node: child sums read (40),
+                                                         # sums (40) and child list (32) written,
+                                                         # the FP64 record set (FP64 + FP32
+                                                         # records: 80)
     }
     tree.set_phase_timing(True)
     phase_runs = []
@@ -439,7 +442,8 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
     import torch
 
     from nbody import generators, workloads
-    from nbody.lib import SYM_AUTO, SYM_NEVER, fma_peak, set_naive_symmetric
+    from nbody.lib import (REC_DF, REC_FP64, SYM_AUTO, SYM_NEVER, fma_peak,
+                           set_naive_symmetric)
 
     out = {}
 
@@ -459,13 +463,16 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
     def bh32():
         tree.build(m, *pos, G)
         tree.accel(*pos, *acc, G, EPS2, "group", "f32c")
+    tree.set_records(0)  # the FP32 group rule reads only the FP32 records
     ms = timed(bh32, 10)
+    tree.set_records(REC_FP64)
     out["bh_f32c_group_theta0.5_1M"] = {"build_plus_traversal_ms": ms, "steps_per_s": 1e3 / ms}
     # the headline step with the double-float traversal (NB_DF64: same accepted cells, monopoles
     # in FP32-pair arithmetic) on a copy of the state, and its force difference to FP64
     pos2 = [p.clone() for p in pos]
     acc64 = [a.clone() for a in acc]
     acc2 = [torch.zeros_like(a) for a in acc]
+    tree.set_records(REC_FP64 | REC_DF)  # the double-float traversal also reads the DF records
     tree.build(m, *pos2, G)
     tree.accel(*pos2, *acc64, G, EPS2, "theta", "f64")
     tree.accel(*pos2, *acc2, G, EPS2, "theta", "df64")
@@ -478,6 +485,7 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
         tree.accel(*pos2, *acc2, G, EPS2, "theta", "df64")
     ms = timed(bh_df, 10)
     ms_tr = timed(lambda: tree.accel(*pos2, *acc2, G, EPS2, "theta", "df64"), 10)
+    tree.set_records(REC_FP64)
     out["bh_df64_theta0.5_1M"] = {
         "build_plus_traversal_ms": ms, "traversal_ms": ms_tr,
         "steps_per_s_excluding_leapfrog": 1e3 / ms,

@@ -280,6 +280,24 @@ nb_status nb_bh_tree_create(nb_ctx* ctx, uint32_t n_max, const nb_bh_params* par
 nb_status nb_bh_tree_destroy(nb_bh_tree* tree);
 nb_status nb_bh_tree_set_theta(nb_bh_tree* tree, double theta);
 
+/* Node records later builds compute (no reference counterpart: the reference keeps only the
+ * sums). The FP32 records (centres relative to the box centre, G*mass, edge^2) are always built;
+ * further sets by bit:
+ *   NB_REC_FP64    FP64 centres (the IEEE quotients of the reference's sums), masses, edges: the
+ *                  per-body rule in NB_F64_IEEE, NB_F64 and NB_DF64, the FP64 group rule,
+ *                  nb_bh_count_interactions and nb_bh_generate_pairs;
+ *   NB_REC_DF      the further FP32 terms of centres and G*mass (exact triple-floats): NB_DF64;
+ *   NB_REC_LEARNED per-node spread, count and first body, FP32 body copies in tree order:
+ *                  NB_OPEN_LEARNED and nb_bh_generate_pairs.
+ * Default NB_REC_ALL. Without NB_REC_FP64 the FP32 centres come from a reciprocal instead of the
+ * IEEE quotients (within an FP32 rounding of them). A call whose records the last build did not
+ * compute fails with NB_ERR_INVALID_ARG. */
+#define NB_REC_FP64 1u
+#define NB_REC_DF 2u
+#define NB_REC_LEARNED 4u
+#define NB_REC_ALL 7u
+nb_status nb_bh_set_records(nb_bh_tree* tree, unsigned int mask);
+
 /* Replaces BarnesHutOctree::buildOctree (BarnesHutOctree.hpp:102-103;
  * ParallelOctreeTopDownSubtrees.cpp:15-93): AABB, octree, centre of mass, body order.
  * G only scales the FP32 traversal records (masses stay in the caller's units). */

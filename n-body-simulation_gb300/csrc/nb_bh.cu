@@ -117,9 +117,11 @@ constexpr int KT_ENTRIES = (1 << KT_LEVELS) - 1;
 // digits are those of key_word, bit for bit.
 __global__ void __launch_bounds__(BH_THREADS)
 keys_kernel(const double* __restrict__ x, const double* __restrict__ y,
-            const double* __restrict__ z, uint32_t n, const double* __restrict__ box,
+            const double* __restrict__ z, uint32_t n, double* __restrict__ box,
             uint64_t* __restrict__ key0, uint32_t* __restrict__ ids) {
     __shared__ uint64_t mids[3][KT_ENTRIES];
+    if (blockIdx.x == 0 && threadIdx.x < 3)  // box centre, for the node records
+        box[7 + threadIdx.x] = box[threadIdx.x] + box[6] / 2;
     {
         Halving h(box[6]);
         for (int L = 0; L < KT_LEVELS; ++L) {
@@ -351,6 +353,7 @@ __global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
 
 struct ComArgs {
     uint32_t n;
+    uint32_t records;  // NB_REC_* sets to compute
     const double *m, *x, *y, *z;
     const double* box;
     double G;
@@ -377,22 +380,43 @@ __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double 
                               double sm, double qsum, uint32_t count, int level, uint32_t skip,
                               uint32_t body) {
     const double edge = ldexp(A.box[6], -level);
-    NodeRec64 r;
-    r.cx = sm != 0 ? __ddiv_rn(cx, sm) : 0.0;  // massless cells: finite centre (never used)
-    r.cy = sm != 0 ? __ddiv_rn(cy, sm) : 0.0;
-    r.cz = sm != 0 ? __ddiv_rn(cz, sm) : 0.0;
-    r.mass = sm;
-    r.edge = edge;
-    r.skip = skip;
-    r.body = body;
-    A.rec64[idx] = r;
-    NodeRec32 q;
+    const double ox = A.box[7], oy = A.box[8], oz = A.box[9];  // box centre
+    // centre = sums / mass: the IEEE quotients when the FP64 records are built (the reference's
+    // values, also behind the FP32 pre-test's proven margin), else from one reciprocal (the FP32
+    // records round it); massless cells get a finite centre (never used)
+    double rcx = 0.0, rcy = 0.0, rcz = 0.0, inv = 0.0;
     if (sm != 0) {
-        const double ox = A.box[0] + A.box[6] / 2, oy = A.box[1] + A.box[6] / 2,
-                     oz = A.box[2] + A.box[6] / 2;
-        q.cx = (float)(r.cx - ox);
-        q.cy = (float)(r.cy - oy);
-        q.cz = (float)(r.cz - oz);
+        // 1/M from the hardware estimate and one Newton step (~2^-44: ample for the FP32
+        // centres and the spread)
+        asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(inv) : "d"(sm));
+        inv = inv * fma(-sm, inv, 2.0);
+        if (A.records & NB_REC_FP64) {
+            rcx = __ddiv_rn(cx, sm);
+            rcy = __ddiv_rn(cy, sm);
+            rcz = __ddiv_rn(cz, sm);
+        } else {
+            rcx = cx * inv;
+            rcy = cy * inv;
+            rcz = cz * inv;
+        }
+    }
+    if (A.records & NB_REC_FP64) {
+        NodeRec64 r;
+        r.cx = rcx;
+        r.cy = rcy;
+        r.cz = rcz;
+        r.mass = sm;
+        r.edge = edge;
+        r.skip = skip;
+        r.body = body;
+        A.rec64[idx] = r;
+    }
+    NodeRec32 q;
+    const double gx = rcx - ox, gy = rcy - oy, gz = rcz - oz;
+    if (sm != 0) {
+        q.cx = (float)gx;
+        q.cy = (float)gy;
+        q.cz = (float)gz;
     } else {  // massless cell: far away, contributes exactly 0
         q.cx = q.cy = q.cz = 1e30f;
     }
@@ -402,40 +426,36 @@ __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double 
     q.body = body;
     q.level = (uint32_t)level;
     A.rec32[idx] = q;
-    // further FP32 terms: the centre minus the box centre, exactly, as a triple-float (rec32,
-    // rec32lo, rec32lo2 .xyz) and G*mass as a double-float (rec32.gm, rec32lo.w)
-    float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), lo2 = lo;
-    if (sm != 0) {
-        const double ox = A.box[0] + A.box[6] / 2, oy = A.box[1] + A.box[6] / 2,
-                     oz = A.box[2] + A.box[6] / 2;
-        float hx, hy, hz;  // equal to q.cx, q.cy, q.cz (both round the same FP64 difference)
-        tf_split_diff(r.cx, ox, hx, lo.x, lo2.x);
-        tf_split_diff(r.cy, oy, hy, lo.y, lo2.y);
-        tf_split_diff(r.cz, oz, hz, lo.z, lo2.z);
-        lo.w = (float)(A.G * sm - (double)q.gm);
+    if (A.records & NB_REC_DF) {
+        // further FP32 terms: the centre minus the box centre, exactly, as a triple-float (rec32,
+        // rec32lo, rec32lo2 .xyz) and G*mass as a double-float (rec32.gm, rec32lo.w)
+        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), lo2 = lo;
+        if (sm != 0) {
+            float hx, hy, hz;  // equal to q.cx, q.cy, q.cz (both round the same FP64 difference)
+            tf_split_diff(rcx, ox, hx, lo.x, lo2.x);
+            tf_split_diff(rcy, oy, hy, lo.y, lo2.y);
+            tf_split_diff(rcz, oz, hz, lo.z, lo2.z);
+            lo.w = (float)(A.G * sm - (double)q.gm);
+        }
+        A.rec32lo[idx] = lo;
+        A.rec32lo2[idx] = lo2;
     }
-    A.rec32lo[idx] = lo;
-    A.rec32lo2[idx] = lo2;
-    // spread^2 = sum m |x-o|^2 / M - |c-o|^2 (o = box centre, which keeps both terms small)
-    NodeAux x;
-    if (sm != 0) {
-        const double ox = A.box[0] + A.box[6] / 2, oy = A.box[1] + A.box[6] / 2,
-                     oz = A.box[2] + A.box[6] / 2;
-        const double gx = r.cx - ox, gy = r.cy - oy, gz = r.cz - oz;
-        // 1/M from the hardware estimate and one Newton step (~2^-44: the spread is a feature of
-        // the learned policy, not a sum of the reference), the root in FP32
-        double inv;
-        asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(inv) : "d"(sm));
-        inv = inv * fma(-sm, inv, 2.0);
-        const double s2 = qsum * inv - (gx * gx + gy * gy + gz * gz);
-        x.spread = sqrtf((float)(s2 > 0 ? s2 : 0.0));
-    } else {
-        x.spread = 0.f;
+    if (A.records & NB_REC_LEARNED) {
+        // spread^2 = sum m |x-o|^2 / M - |c-o|^2 (o = box centre, which keeps both terms small);
+        // the spread is a feature of the learned policy, not a sum of the reference: 1/M from the
+        // reciprocal, the root in FP32
+        NodeAux x;
+        if (sm != 0) {
+            const double s2 = qsum * inv - (gx * gx + gy * gy + gz * gz);
+            x.spread = sqrtf((float)(s2 > 0 ? s2 : 0.0));
+        } else {
+            x.spread = 0.f;
+        }
+        x.count = count;
+        x.first = A.node_first_pos[idx];
+        x.edge = (float)edge;
+        A.aux[idx] = x;
     }
-    x.count = count;
-    x.first = A.node_first_pos[idx];
-    x.edge = (float)edge;
-    A.aux[idx] = x;
 }
 
 __global__ void com_kernel(ComArgs A) {
@@ -444,21 +464,22 @@ __global__ void com_kernel(ComArgs A) {
     const uint32_t idx = A.base[p] + __popcll(A.mask[p]);
     const uint32_t b = A.ids[p];
     const double mb = A.m[b];
-    const double cx = __dmul_rn(A.x[b], mb), cy = __dmul_rn(A.y[b], mb), cz = __dmul_rn(A.z[b], mb);
-    const double ox = A.box[0] + A.box[6] / 2, oy = A.box[1] + A.box[6] / 2,
-                 oz = A.box[2] + A.box[6] / 2;
-    const double rx = A.x[b] - ox, ry = A.y[b] - oy, rz = A.z[b] - oz;
-    const double qb = mb * (rx * rx + ry * ry + rz * rz);
+    const double bx = A.x[b], by = A.y[b], bz = A.z[b];
+    const double cx = __dmul_rn(bx, mb), cy = __dmul_rn(by, mb), cz = __dmul_rn(bz, mb);
+    const bool learned = (A.records & NB_REC_LEARNED) != 0;
     A.comx[idx] = cx;
     A.comy[idx] = cy;
     A.comz[idx] = cz;
     A.mass[idx] = mb;
-    A.q[idx] = qb;
     A.node_count[idx] = 1;
-    const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
-    A.sorted4[p] = make_float4(hx, hy, hz, (float)(A.G * mb));
-    A.sorted4lo[p] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy),
-                                 (float)(rz - (double)hz), 0.f);
+    if (learned) {  // spread sums and the FP32 body copies of the learned policy
+        const double rx = bx - A.box[7], ry = by - A.box[8], rz = bz - A.box[9];
+        A.q[idx] = mb * (rx * rx + ry * ry + rz * rz);
+        const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
+        A.sorted4[p] = make_float4(hx, hy, hz, (float)(A.G * mb));
+        A.sorted4lo[p] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy),
+                                     (float)(rz - (double)hz), 0.f);
+    }
     uint32_t cur = A.node_parent[idx];
     while (cur != NB_NONE) {
         // acquire-release arrival: publishes this child's sums and, for the last child, makes
@@ -489,14 +510,14 @@ __global__ void com_kernel(ComArgs A) {
             sy = __dadd_rn(sy, __ldcg(&A.comy[ch]));
             sz = __dadd_rn(sz, __ldcg(&A.comz[ch]));
             sm = __dadd_rn(sm, __ldcg(&A.mass[ch]));
-            sq += __ldcg(&A.q[ch]);
+            if (learned) sq += __ldcg(&A.q[ch]);
             count += __ldcg(&A.node_count[ch]);
         }
         A.comx[cur] = sx;
         A.comy[cur] = sy;
         A.comz[cur] = sz;
         A.mass[cur] = sm;
-        A.q[cur] = sq;
+        if (learned) A.q[cur] = sq;
         A.node_count[cur] = count;
         cur = A.node_parent[cur];
     }
@@ -508,8 +529,9 @@ __global__ void com_kernel(ComArgs A) {
 __global__ void records_kernel(ComArgs A, const uint32_t* __restrict__ info) {
     const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= info[0]) return;
-    write_records(A, idx, A.comx[idx], A.comy[idx], A.comz[idx], A.mass[idx], A.q[idx],
-                  A.node_count[idx], A.node_level[idx], A.node_skip[idx], A.node_body[idx]);
+    write_records(A, idx, A.comx[idx], A.comy[idx], A.comz[idx], A.mass[idx],
+                  (A.records & NB_REC_LEARNED) ? A.q[idx] : 0.0, A.node_count[idx],
+                  A.node_level[idx], A.node_skip[idx], A.node_body[idx]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -714,6 +736,7 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     NB_TRY(mark(4));
     ComArgs A;
     A.n = n;
+    A.records = t->records;
     A.m = m;
     A.x = x;
     A.y = y;
@@ -753,6 +776,15 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     NB_TRY(nb::check_launch("records_kernel"));
     NB_TRY(mark(5));
     t->built = true;
+    t->built_records = t->records;
+    return NB_OK;
+}
+
+nb_status nb_bh_set_records(nb_bh_tree* t, unsigned int mask) {
+    if (!t) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_set_records: null tree");
+    if (mask & ~NB_REC_ALL)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_set_records: unknown bits 0x%x", mask);
+    t->records = mask;
     return NB_OK;
 }
 

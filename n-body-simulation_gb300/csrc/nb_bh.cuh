@@ -50,6 +50,8 @@ struct nb_bh_tree {
     uint32_t* work = nullptr;  // work counter of persistent traversal kernels
     cudaEvent_t phase_ev[6] = {};  // build phase boundaries (nb_bh_set_phase_timing)
     bool phase_timing = false;
+    uint32_t records = NB_REC_ALL;   // record sets the next build computes (nb_bh_set_records)
+    uint32_t built_records = 0;      // record sets of the last build
 
     uint64_t *key0 = nullptr, *key1 = nullptr, *key_alt = nullptr;
     uint32_t *ids = nullptr, *ids_alt = nullptr;
@@ -82,6 +84,16 @@ struct nb_bh_tree {
     float policy_theta = 0.5f;
     uint32_t policy_count_cap = 8192;
 };
+
+// NB_OK when the last build computed the record sets `need` (NB_REC_*), else an error naming
+// `what`.
+inline nb_status nb_need_records(const nb_bh_tree* t, uint32_t need, const char* what) {
+    if ((t->built_records & need) == need) return NB_OK;
+    return nb::set_error(NB_ERR_INVALID_ARG,
+                         "%s: the tree was built without the node records it needs (records "
+                         "0x%x built, 0x%x needed; nb_bh_set_records)",
+                         what, t->built_records, need);
+}
 
 // Digit maps between the reference's octant index o = 4*(y>mid) + 2*(x>mid) + (z<mid) and the
 // visit rank t (the reference pushes children 5,7,4,6,1,3,0,2 and pops 2,0,3,1,6,4,7,5).

@@ -626,6 +626,7 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
     if (opening == NB_OPEN_THETA) {
         switch (prec) {
             case NB_F64_IEEE:
+                NB_TRY(nb_need_records(t, NB_REC_FP64, "nb_bh_accel"));
                 if (g_lockstep) {
                     bh_theta_f64_kernel<IEEE64><<<grid, TR_THREADS, 0, s>>>(
                         t->rec64, t->info, t->ids, x, y, z, n, theta, eps2, G, ax, ay, az);
@@ -633,6 +634,7 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
                 }
                 return launch_lane<IEEE64>(ctx, t, x, y, z, ax, ay, az, G, eps2, s);
             case NB_F64:
+                NB_TRY(nb_need_records(t, NB_REC_FP64, "nb_bh_accel"));
                 if (g_lockstep) {
                     bh_theta_f64_kernel<FAST64><<<grid, TR_THREADS, 0, s>>>(
                         t->rec64, t->info, t->ids, x, y, z, n, theta, eps2, G, ax, ay, az);
@@ -640,6 +642,7 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
                 }
                 return launch_lane<FAST64>(ctx, t, x, y, z, ax, ay, az, G, eps2, s);
             case NB_DF64:
+                NB_TRY(nb_need_records(t, NB_REC_FP64 | NB_REC_DF, "nb_bh_accel"));
                 if (t->G == 0)
                     return nb::set_error(NB_ERR_INVALID_ARG,
                                          "nb_bh_accel: NB_DF64 needs a build with G != 0");
@@ -661,6 +664,7 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
         switch (prec) {
             case NB_F64_IEEE:
             case NB_F64:
+                NB_TRY(nb_need_records(t, NB_REC_FP64, "nb_bh_accel"));
                 bh_group_f64_kernel<<<grid, TR_THREADS, 0, s>>>(t->rec64, t->info, t->ids, x, y, z,
                                                                 n, theta, eps2, G, ax, ay, az);
                 return nb::check_launch("bh_group_f64_kernel");
@@ -679,6 +683,7 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
             return nb::set_error(NB_ERR_UNSUPPORTED, "nb_bh_accel: NB_OPEN_LEARNED runs in NB_F32C");
         if (G != t->G)
             return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: G differs from the build's");
+        NB_TRY(nb_need_records(t, NB_REC_LEARNED, "nb_bh_accel"));
         return nb::launch_learned(ctx, t, x, y, z, ax, ay, az, eps2, nullptr, s);
     }
     return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: unknown opening %d / precision %d",
@@ -693,6 +698,7 @@ nb_status nb_bh_count_interactions(nb_ctx* ctx, const nb_bh_tree* t, const doubl
     if (!x || !y || !z || !out_dev) return nb::set_error(NB_ERR_INVALID_ARG, "null pointer");
     if (opening != NB_OPEN_THETA && opening != NB_OPEN_THETA_GROUP)
         return nb::set_error(NB_ERR_UNSUPPORTED, "nb_bh_count_interactions: theta rules only");
+    NB_TRY(nb_need_records(t, NB_REC_FP64, "nb_bh_count_interactions"));
     cudaStream_t s = (cudaStream_t)stream_;
     NB_CUDA_TRY(cudaMemsetAsync(out_dev, 0, 2 * sizeof(unsigned long long), s));
     bh_count_kernel<<<nb::ceil_div(t->n, TR_THREADS), TR_THREADS, 0, s>>>(
@@ -708,6 +714,7 @@ nb_status nb_bh_accel_learned_counted(nb_ctx* ctx, const nb_bh_tree* t, const do
     NB_CHECK_CTX(ctx);
     if (!t || !t->built) return nb::set_error(NB_ERR_NOT_BUILT, "tree not built");
     if (!counters_dev) return nb::set_error(NB_ERR_INVALID_ARG, "null counters");
+    NB_TRY(nb_need_records(t, NB_REC_LEARNED, "nb_bh_accel_learned_counted"));
     NB_CUDA_TRY(cudaMemsetAsync(counters_dev, 0, 2 * sizeof(unsigned long long), (cudaStream_t)stream));
     return nb::launch_learned(ctx, t, x, y, z, ax, ay, az, eps2, counters_dev, (cudaStream_t)stream);
 }

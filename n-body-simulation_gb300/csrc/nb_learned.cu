@@ -955,6 +955,7 @@ nb_status nb_bh_generate_pairs(nb_ctx* ctx, const nb_bh_tree* t, const double* m
                                uint32_t* pairs_out, nb_stream_t stream) {
     NB_CHECK_CTX(ctx);
     if (!t || !t->built) return nb::set_error(NB_ERR_NOT_BUILT, "nb_bh_generate_pairs: tree not built");
+    NB_TRY(nb_need_records(t, NB_REC_FP64 | NB_REC_LEARNED, "nb_bh_generate_pairs"));
     if (!m || !x || !y || !z || !ax || !ay || !az || !features || !labels || !count_dev ||
         max_pairs == 0 || !(sample_fraction > 0) || sample_fraction > 1)
         return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_generate_pairs: bad arguments");

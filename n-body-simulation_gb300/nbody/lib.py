@@ -222,6 +222,7 @@ SIGNATURES.update({
     "nb_naive_accel_targets": [_vp] + [_vp] * 4 + [_u32, _vp, _u32] + [_vp] * 3 + [_d, _d, _vp],
     "nb_bh_set_policy": [_vp, _vp, C.c_float, _d, _u32, _u32],
     "nb_bh_set_phase_timing": [_vp, _i],
+    "nb_bh_set_records": [_vp, C.c_uint],
     "nb_bh_graph_create": [_vp, _vp] + [_vp] * 13 + [_u32, _d, _d, _d, _i, _i, _i, _vp],
     "nb_bh_build_phase_ms": [_vp, _vp],
     "nb_bh_accel_learned_counted": [_vp, _vp] + [_vp] * 6 + [_d, _vp, _vp],
@@ -273,6 +274,10 @@ class BHTree:
                                           m.numel(), G, eps2, dt, steps, OPENINGS[opening],
                                           PRECISIONS[precision], C.byref(h)))
         return Graph(h)
+
+    def set_records(self, mask):
+        """Node record sets later builds compute (REC_* bits; records_for gives a traversal's)."""
+        check(self.lib.nb_bh_set_records(self.handle, mask))
 
     def set_phase_timing(self, enable=True):
         check(self.lib.nb_bh_set_phase_timing(self.handle, 1 if enable else 0))
@@ -408,6 +413,21 @@ def set_naive_pair_config(config: int):
 
 
 SYM_NEVER, SYM_AUTO, SYM_ALWAYS = 0, 1, 2
+
+# node record sets of a tree build (NB_REC_*)
+REC_FP64, REC_DF, REC_LEARNED = 1, 2, 4
+REC_ALL = REC_FP64 | REC_DF | REC_LEARNED
+
+
+def records_for(opening: str, precision: str) -> int:
+    """The record sets nb_bh_accel needs for an opening rule and precision."""
+    if opening == "learned":
+        return REC_LEARNED
+    if precision == "f32c":
+        return 0
+    if precision == "df64":
+        return REC_FP64 | REC_DF
+    return REC_FP64
 
 
 def set_naive_symmetric(mode: int = SYM_AUTO, config: int = 0, config_f64: int = 0,

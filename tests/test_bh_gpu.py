@@ -323,3 +323,72 @@ def test_graph_create_rejects_phase_timing_and_bad_steps(ctx):
     ctx.sync()
     g.close()
     t.close()
+
+
+# -- node record sets -------------------------------------------------------------------------------
+@pytest.mark.parametrize("opening,precision", [("theta", "f64_ieee"), ("theta", "f64"),
+                                               ("theta", "df64"), ("group", "f64"),
+                                               ("theta", "f32c"), ("group", "f32c")])
+def test_record_sets_give_the_same_forces(ctx, opening, precision):
+    """A build with only the records a traversal reads (records_for) gives that traversal the
+    forces of a build with all records: bit for bit for the FP64 rules (the FP64 centres are the
+    same IEEE quotients), within FP32 rounding of the centres for f32c (which then rounds a
+    reciprocal-based centre)."""
+    from nbody.lib import REC_ALL, records_for
+    d = bodies("disc", 6000, seed=8)
+    full, dd = build(ctx, d, theta=0.5)
+    ref = accel(ctx, full, dd, d["G"], 1e-22, opening, precision)
+    lean, _ = build(ctx, d, theta=0.5)
+    lean.set_records(records_for(opening, precision))
+    lean.build(dd["m"], dd["x"], dd["y"], dd["z"], d["G"])
+    got = accel(ctx, lean, dd, d["G"], 1e-22, opening, precision)
+    if precision == "f32c":
+        assert np.median(rel_err(*got, *ref)) <= 1e-6
+    else:
+        for g, r in zip(got, ref):
+            np.testing.assert_array_equal(g, r)
+    assert records_for(opening, precision) != REC_ALL
+    full.close()
+    lean.close()
+
+
+def test_missing_records_are_rejected(ctx):
+    """Traversals that read records the last build did not compute fail with INVALID_ARG."""
+    import torch
+    from nbody.lib import REC_FP64, NBodyError
+    d = bodies("plummer", 3000, seed=9)
+    t, dd = build(ctx, d, theta=0.5)
+    t.set_records(0)
+    t.build(dd["m"], dd["x"], dd["y"], dd["z"], d["G"])
+    a = [torch.zeros(3000, dtype=torch.float64, device="cuda") for _ in range(3)]
+    for opening, precision in (("theta", "f64"), ("theta", "f64_ieee"), ("theta", "df64"),
+                               ("group", "f64"), ("learned", "f32c")):
+        with pytest.raises(NBodyError, match="INVALID_ARG"):
+            t.accel(dd["x"], dd["y"], dd["z"], *a, d["G"], 1e-6, opening, precision)
+    with pytest.raises(NBodyError, match="INVALID_ARG"):
+        t.count_interactions(dd["x"], dd["y"], dd["z"], "theta")
+    t.accel(dd["x"], dd["y"], dd["z"], *a, d["G"], 1e-6, "group", "f32c")  # FP32 records only
+    t.set_records(REC_FP64)
+    t.build(dd["m"], dd["x"], dd["y"], dd["z"], d["G"])
+    t.accel(dd["x"], dd["y"], dd["z"], *a, d["G"], 1e-6, "theta", "f64")
+    ctx.sync()
+    with pytest.raises(NBodyError, match="INVALID_ARG"):
+        t.set_records(8)
+    t.close()
+
+
+def test_learned_walk_on_learned_records(ctx):
+    """The learned traversal's walk (group theta rule in place of the network) on a build with
+    only the learned records agrees with a build with all records to FP32 rounding."""
+    from nbody.lib import REC_LEARNED
+    d = bodies("disc", 6000, seed=10)
+    res = []
+    for mask in (None, REC_LEARNED):
+        t, dd = build(ctx, d, theta=0.5)
+        if mask is not None:
+            t.set_records(mask)
+            t.build(dd["m"], dd["x"], dd["y"], dd["z"], d["G"])
+        t.set_policy(None, 0.0, 0.4, 2 ** 31 - 1)
+        res.append(accel(ctx, t, dd, d["G"], 1e-22, "learned", "f32c"))
+        t.close()
+    assert np.median(rel_err(*res[1], *res[0])) <= 1e-6
