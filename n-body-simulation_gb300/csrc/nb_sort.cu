@@ -117,6 +117,7 @@ constexpr uint32_t LB_AGGREGATE = 1u << 30;
 constexpr uint32_t LB_TOTAL = 2u << 30;
 constexpr uint32_t LB_VALUE = (1u << 30) - 1u;
 constexpr unsigned long long LB_WAIT_LIMIT = 1ull << 22;
+constexpr int LB_WINDOW = 8;  // predecessor words read per look-back round trip
 
 // hist[p][d]: keys whose digit of pass p is d, for all passes in one read.
 __global__ void __launch_bounds__(RS_THREADS)
@@ -210,21 +211,33 @@ radix_pass_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restri
             lb_store(mine, LB_TOTAL | run);
         } else {
             lb_store(mine, LB_AGGREGATE | run);
-            bool timed_out = false;
-            for (uint32_t t = tile; t-- > 0;) {
-                const uint32_t* w = lb + (size_t)t * RS_BINS + d;
-                uint32_t v = lb_load(w);
-                for (unsigned long long it = 0; (v & (LB_AGGREGATE | LB_TOTAL)) == 0; ++it) {
-                    if (it >= LB_WAIT_LIMIT) {
-                        timed_out = true;
+            // walk back in windows of LB_WINDOW predecessors, their words loaded together (one
+            // round trip per window), up to the nearest published total (tile 0 always has one)
+            bool timed_out = false, done = false;
+            for (int t0 = (int)tile - 1; !done && t0 >= 0; t0 -= LB_WINDOW) {
+                uint32_t v[LB_WINDOW];
+#pragma unroll
+                for (int j = 0; j < LB_WINDOW; ++j)
+                    v[j] = t0 - j >= 0 ? lb_load(lb + (size_t)(t0 - j) * RS_BINS + d) : 0u;
+#pragma unroll
+                for (int j = 0; j < LB_WINDOW; ++j) {
+                    if (done || t0 - j < 0) break;
+                    const uint32_t* w = lb + (size_t)(t0 - j) * RS_BINS + d;
+                    for (unsigned long long it = 0; (v[j] & (LB_AGGREGATE | LB_TOTAL)) == 0; ++it) {
+                        if (it >= LB_WAIT_LIMIT) {
+                            timed_out = true;
+                            break;
+                        }
+                        __nanosleep(32);
+                        v[j] = lb_load(w);
+                    }
+                    if (timed_out) {
+                        done = true;
                         break;
                     }
-                    __nanosleep(32);
-                    v = lb_load(w);
+                    before += v[j] & LB_VALUE;
+                    if (v[j] & LB_TOTAL) done = true;
                 }
-                if (timed_out) break;
-                before += v & LB_VALUE;
-                if (v & LB_TOTAL) break;
             }
             if (timed_out) atomicOr(err, NB_DEVERR_TIMEOUT);
             lb_store(mine, LB_TOTAL | (before + run));
