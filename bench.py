@@ -442,7 +442,7 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
     import torch
 
     from nbody import generators, workloads
-    from nbody.lib import (REC_DF, REC_FP64, SYM_AUTO, SYM_NEVER, fma_peak,
+    from nbody.lib import (REC_DF, REC_FP64, SYM_AUTO, SYM_NEVER, build_mask_for, fma_peak,
                            set_naive_symmetric)
 
     out = {}
@@ -463,7 +463,7 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
     def bh32():
         tree.build(m, *pos, G)
         tree.accel(*pos, *acc, G, EPS2, "group", "f32c")
-    tree.set_records(0)  # the FP32 group rule reads only the FP32 records
+    tree.set_records(build_mask_for("group", "f32c"))  # FP32 records, quantized keys
     ms = timed(bh32, 10)
     tree.set_records(REC_FP64)
     out["bh_f32c_group_theta0.5_1M"] = {"build_plus_traversal_ms": ms, "steps_per_s": 1e3 / ms}

@@ -291,11 +291,17 @@ nb_status nb_bh_tree_set_theta(nb_bh_tree* tree, double theta);
  *                  NB_OPEN_LEARNED and nb_bh_generate_pairs.
  * Default NB_REC_ALL. Without NB_REC_FP64 the FP32 centres come from a reciprocal instead of the
  * IEEE quotients (within an FP32 rounding of them). A call whose records the last build did not
- * compute fails with NB_ERR_INVALID_ARG. */
+ * compute fails with NB_ERR_INVALID_ARG.
+ * NB_BUILD_QUANTIZED_KEYS (same mask; for runs whose forces need no reference-exact cells, such
+ * as the FP32 and learned rules): bodies are placed by 42-bit quantized coordinates instead of
+ * the reference's FP64 midpoint recurrence (BarnesHutOctree.cpp, ParallelOctreeTopDownSubtrees
+ * .cpp:219-428); the cells then differ from the reference's only for bodies within FP64 rounding
+ * of a cell midpoint. Off by default. */
 #define NB_REC_FP64 1u
 #define NB_REC_DF 2u
 #define NB_REC_LEARNED 4u
 #define NB_REC_ALL 7u
+#define NB_BUILD_QUANTIZED_KEYS 8u
 nb_status nb_bh_set_records(nb_bh_tree* tree, unsigned int mask);
 
 /* Replaces BarnesHutOctree::buildOctree (BarnesHutOctree.hpp:102-103;

@@ -169,12 +169,57 @@ keys_kernel(const double* __restrict__ x, const double* __restrict__ y,
     }
 }
 
+// Quantized keys (NB_BUILD_QUANTIZED_KEYS): every coordinate as a 42-bit fraction of the box,
+// floor((v - min) * 2^42 / edge), one bit per level. Bodies fall into the cells of the
+// reference's recurrence except within FP64 rounding of a cell midpoint (there the quantized
+// rule puts them in the upper half). Bits interleave with the usual 3-way spread, the digits
+// already in visit order: visit rank = 4 * (y upper) + 2 * (z lower) + (x lower).
+__device__ __forceinline__ uint64_t spread3(uint64_t v) {  // bit i -> bit 3i, i < 21
+    v &= 0x1fffffull;
+    v = (v | v << 32) & 0x1f00000000ffffull;
+    v = (v | v << 16) & 0x1f0000ff0000ffull;
+    v = (v | v << 8) & 0x100f00f00f00f00full;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+    v = (v | v << 2) & 0x1249249249249249ull;
+    return v;
+}
+
+__device__ __forceinline__ uint64_t quantize42(double v, double mn, double scale) {
+    const double q = (v - mn) * scale;
+    const uint64_t top = (1ull << 42) - 1;
+    if (!(q > 0.0)) return 0;
+    const uint64_t u = __double2ull_rz(q);
+    return u > top ? top : u;
+}
+
+__device__ uint64_t key_word_quantized(const double* __restrict__ box, double px, double py,
+                                       double pz, int word) {
+    const double scale = box[6] > 0.0 ? 4398046511104.0 / box[6] : 0.0;  // 2^42 / edge
+    const uint64_t ix = quantize42(px, box[0], scale), iy = quantize42(py, box[1], scale),
+                   iz = quantize42(pz, box[2], scale);
+    const int shift = word == 0 ? NB_KEY_LEVELS : 0;
+    const uint64_t m = 0x1fffffull;
+    const uint64_t hx = (ix >> shift) & m, hy = (iy >> shift) & m, hz = (iz >> shift) & m;
+    return (spread3(hy) << 2) | (spread3(~hz & m) << 1) | spread3(~hx & m);
+}
+
+__global__ void keys_quantized_kernel(const double* __restrict__ x, const double* __restrict__ y,
+                                      const double* __restrict__ z, uint32_t n,
+                                      double* __restrict__ box, uint64_t* __restrict__ key0,
+                                      uint32_t* __restrict__ ids) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 3) box[7 + i] = box[i] + box[6] / 2;  // box centre, for the node records
+    if (i >= n) return;
+    key0[i] = key_word_quantized(box, x[i], y[i], z[i], 0);
+    ids[i] = i;
+}
+
 // Runs of equal first words: compute the second word and insertion-sort the run (stable).
 __global__ void runs_fixup_kernel(const double* __restrict__ x, const double* __restrict__ y,
                                   const double* __restrict__ z, uint32_t n,
                                   const double* __restrict__ box, const uint64_t* __restrict__ key0,
                                   uint64_t* __restrict__ key1, uint32_t* __restrict__ ids,
-                                  uint32_t* __restrict__ err) {
+                                  uint32_t* __restrict__ err, int quantized) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p + 1 >= n) return;
     const uint64_t k = key0[p];
@@ -188,7 +233,8 @@ __global__ void runs_fixup_kernel(const double* __restrict__ x, const double* __
     }
     for (uint32_t q = p; q < p + r; ++q) {
         const uint32_t b = ids[q];
-        key1[q] = key_word(box, x[b], y[b], z[b], 1);
+        key1[q] = quantized ? key_word_quantized(box, x[b], y[b], z[b], 1)
+                            : key_word(box, x[b], y[b], z[b], 1);
     }
     for (uint32_t q = p + 1; q < p + r; ++q) {  // insertion sort, stable
         const uint64_t kk = key1[q];
@@ -698,9 +744,14 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     NB_TRY(mark(0));
     NB_TRY(nb::launch_aabb(ctx, x, y, z, n, t->box, s));
     NB_TRY(mark(1));
-    // persistent blocks: each evaluates the midpoint table once, then walks its bodies
-    keys_kernel<<<std::min(grid, 8 * ctx->sm_count), BH_THREADS, 0, s>>>(x, y, z, n, t->box,
-                                                                        t->key0, t->ids);
+    const bool quantized = (t->records & NB_BUILD_QUANTIZED_KEYS) != 0;
+    if (quantized) {
+        keys_quantized_kernel<<<grid, BH_THREADS, 0, s>>>(x, y, z, n, t->box, t->key0, t->ids);
+    } else {
+        // persistent blocks: each evaluates the midpoint table once, then walks its bodies
+        keys_kernel<<<std::min(grid, 8 * ctx->sm_count), BH_THREADS, 0, s>>>(x, y, z, n, t->box,
+                                                                            t->key0, t->ids);
+    }
     NB_TRY(nb::check_launch("keys_kernel"));
     NB_TRY(mark(2));
     int in_alt = 0;
@@ -713,7 +764,7 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     NB_TRY(mark(3));
     NB_CUDA_TRY(cudaMemsetAsync(t->key1, 0, (size_t)n * 8, s));
     runs_fixup_kernel<<<grid, BH_THREADS, 0, s>>>(x, y, z, n, t->box, t->key0, t->key1, t->ids,
-                                                  ctx->dev_error);
+                                                  ctx->dev_error, quantized ? 1 : 0);
     NB_TRY(nb::check_launch("runs_fixup_kernel"));
     NB_CUDA_TRY(cudaMemsetAsync(t->mask, 0, (size_t)n * 8, s));
     splits_kernel<<<grid, BH_THREADS, 0, s>>>(t->key0, t->key1, n, t->split_level, t->split_start,
@@ -782,7 +833,7 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
 
 nb_status nb_bh_set_records(nb_bh_tree* t, unsigned int mask) {
     if (!t) return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_set_records: null tree");
-    if (mask & ~NB_REC_ALL)
+    if (mask & ~(NB_REC_ALL | NB_BUILD_QUANTIZED_KEYS))
         return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_set_records: unknown bits 0x%x", mask);
     t->records = mask;
     return NB_OK;

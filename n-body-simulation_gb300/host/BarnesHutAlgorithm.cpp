@@ -50,9 +50,9 @@ void BarnesHutAlgorithm::startSimulation(const SimulationData& d) {
     p.sort_bodies = configuration::barnes_hut_algorithm::sortBodies ? 1 : 0;
     nb_throw_if(nb_bh_tree_create(ctx, n, &p, &octree), "nb_bh_tree_create");
     // only the node records this run's traversal reads: FP64 centres for the FP64 rules (and the
-    // double-float terms for df64); none beyond the FP32 records for f32c
+    // double-float terms for df64); for f32c none beyond the FP32 records, and quantized keys
     const nb_precision prec = precisionMode();
-    unsigned int records = prec == NB_F32C ? 0u : NB_REC_FP64;
+    unsigned int records = prec == NB_F32C ? NB_BUILD_QUANTIZED_KEYS : NB_REC_FP64;
     if (prec == NB_DF64) records |= NB_REC_DF;
     nb_throw_if(nb_bh_set_records(octree, records), "nb_bh_set_records");
 

@@ -18,7 +18,8 @@ import time
 import numpy as np
 
 from . import generators
-from .lib import REC_LEARNED, BHTree, Context, MLP_PARAMS, mlp_adam, mlp_loss_grad, records_for
+from .lib import (BUILD_QUANTIZED_KEYS, REC_LEARNED, BHTree, Context, MLP_PARAMS, build_mask_for,
+                  mlp_adam, mlp_loss_grad)
 
 EPS2 = 1e-22
 
@@ -171,7 +172,7 @@ def sweep(ctx: Context, t: dict, G: float, targets, ref, params, taus, thetas,
     import torch
     n = t["m"].numel()
     tree = BHTree(ctx, n, theta=0.5)
-    tree.set_records(REC_LEARNED)  # the records of the timed learned steps (time_steps)
+    tree.set_records(REC_LEARNED | BUILD_QUANTIZED_KEYS)  # the timed learned steps' build
     tree.build(t["m"], t["x"], t["y"], t["z"], G)
     prev = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
     tree.accel(t["x"], t["y"], t["z"], *prev, G, eps2, "group", "f32c")  # |a| of a previous step
@@ -221,7 +222,7 @@ def time_steps(ctx: Context, t: dict, G: float, steps: int, opening: str, precis
     acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
     vh = [torch.zeros_like(a) for a in acc]
     tree = BHTree(ctx, n, theta=theta)
-    tree.set_records(records_for(opening, precision))  # only what the timed traversal reads
+    tree.set_records(build_mask_for(opening, precision))  # only what the traversal reads
     tree.build(t["m"], *pos, G)
     tree.accel(*pos, *acc, G, eps2, "group", "f32c")  # step 0 accelerations
     if policy is not None:

@@ -414,9 +414,10 @@ def set_naive_pair_config(config: int):
 
 SYM_NEVER, SYM_AUTO, SYM_ALWAYS = 0, 1, 2
 
-# node record sets of a tree build (NB_REC_*)
+# node record sets of a tree build (NB_REC_*) and the quantized-key build option
 REC_FP64, REC_DF, REC_LEARNED = 1, 2, 4
 REC_ALL = REC_FP64 | REC_DF | REC_LEARNED
+BUILD_QUANTIZED_KEYS = 8
 
 
 def records_for(opening: str, precision: str) -> int:
@@ -428,6 +429,13 @@ def records_for(opening: str, precision: str) -> int:
     if precision == "df64":
         return REC_FP64 | REC_DF
     return REC_FP64
+
+
+def build_mask_for(opening: str, precision: str) -> int:
+    """records_for plus quantized keys for the traversals that need no reference-exact cells
+    (every one without FP64 records: the FP32 rules and the learned policy)."""
+    rec = records_for(opening, precision)
+    return rec if rec & REC_FP64 else rec | BUILD_QUANTIZED_KEYS
 
 
 def set_naive_symmetric(mode: int = SYM_AUTO, config: int = 0, config_f64: int = 0,

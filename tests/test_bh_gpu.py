@@ -373,7 +373,7 @@ def test_missing_records_are_rejected(ctx):
     t.accel(dd["x"], dd["y"], dd["z"], *a, d["G"], 1e-6, "theta", "f64")
     ctx.sync()
     with pytest.raises(NBodyError, match="INVALID_ARG"):
-        t.set_records(8)
+        t.set_records(16)
     t.close()
 
 
@@ -392,3 +392,21 @@ def test_learned_walk_on_learned_records(ctx):
         res.append(accel(ctx, t, dd, d["G"], 1e-22, "learned", "f32c"))
         t.close()
     assert np.median(rel_err(*res[1], *res[0])) <= 1e-6
+
+
+def test_quantized_keys_build_the_same_tree(ctx):
+    """Quantized keys place random bodies in the reference's cells (no body lies within FP64
+    rounding of a midpoint here): same node count and bit-identical FP32 forces."""
+    from nbody.lib import BUILD_QUANTIZED_KEYS
+    d = bodies("disc", 20000, seed=12)
+    out = []
+    for mask in (0, BUILD_QUANTIZED_KEYS):
+        t, dd = build(ctx, d, theta=0.5)
+        t.set_records(mask)
+        t.build(dd["m"], dd["x"], dd["y"], dd["z"], d["G"])
+        nodes = t.stats()["node_count"]
+        out.append((nodes, accel(ctx, t, dd, d["G"], 1e-22, "group", "f32c")))
+        t.close()
+    assert out[0][0] == out[1][0]
+    for g, r in zip(out[1][1], out[0][1]):
+        np.testing.assert_array_equal(g, r)
