@@ -1,6 +1,6 @@
 // nb_pair_sym.cu -- symmetric pair kernel: every unordered pair {i, j} of a system is evaluated
 // once and its force is added to both bodies (Newton's third law, a_i += G m_j r_ij / r^3,
-// a_j -= G m_i r_ij / r^3). Two arithmetic forms share the decomposition:
+// a_j -= G m_i r_ij / r^3). Three arithmetic forms share the decomposition:
 //  * FP32 with compensated accumulation (nb_naive_accel NB_F32C over whole systems, and batches):
 //    positions relative to the system's first body and G*m in FP32; per unordered pair 3 sub,
 //    3 FMA for r^2 + eps^2, one MUFU rsqrt, 2 multiplies for r^-3, 2 for the two mass factors and
@@ -23,7 +23,8 @@
 //
 // Inside a unit each lane holds P i bodies in registers and walks the tile in groups of 32 j
 // bodies: at step s lane l pairs its P bodies with j = (l + s) mod 32 of the group, and the j
-// body's running sum moves one lane down after every step (three shuffles), so after 32 steps
+// body's running sum moves one lane down after every step (three shuffles; six for the (hi, lo)
+// sums of the double-float form), so after 32 steps
 // lane l holds the complete sum of body l of the group over the warp's 32 P i bodies, without a
 // reduction tree. The W warps' j sums of a unit are added in warp order through shared memory and
 // written to the unit's own slot of part_j. FP32 i sums are folded into per-body (hi, lo) TwoSum
