@@ -54,3 +54,42 @@ def test_version_and_error_string_without_gpu(cuda_lib):
 def test_null_context_is_rejected_without_touching_the_gpu(cuda_lib):
     cuda_lib.nb_sync.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
     assert cuda_lib.nb_sync(None, None) == 1  # NB_ERR_INVALID_ARG
+
+
+def header_defines():
+    src = open(os.path.join(ROOT, "include", "nbody.h")).read()
+    return {k: int(v.rstrip("u"), 0)
+            for k, v in re.findall(r"#define\s+(NB_[A-Z0-9_]+)\s+([0-9xa-fA-Fu]+)\b", src)}
+
+
+def test_python_constants_match_the_header():
+    """The binding's copies of the header's counts and bit masks agree with include/nbody.h."""
+    import __graft_entry__  # noqa: F401
+    from nbody import lib
+    h = header_defines()
+    pairs = {"NB_PAIR_CONFIG_COUNT": lib.PAIR_CONFIGS, "NB_BATCH_CONFIG_COUNT": lib.BATCH_CONFIGS,
+             "NB_REC_FP64": lib.REC_FP64, "NB_REC_DF": lib.REC_DF,
+             "NB_REC_LEARNED": lib.REC_LEARNED, "NB_REC_ALL": lib.REC_ALL,
+             "NB_BUILD_QUANTIZED_KEYS": lib.BUILD_QUANTIZED_KEYS}
+    for name, value in pairs.items():
+        assert h[name] == value, (name, h[name], value)
+    assert h["NB_BATCH_CONFIG_COUNT"] == h["NB_PAIR_CONFIG_COUNT"] + h["NB_SYM_CONFIG_COUNT"]
+    assert h["NB_REC_ALL"] & h["NB_BUILD_QUANTIZED_KEYS"] == 0
+
+
+def test_record_sets_per_traversal():
+    """records_for / build_mask_for: what each traversal reads, and quantized keys exactly for
+    the traversals without FP64 records (no reference-exact cells needed)."""
+    import __graft_entry__  # noqa: F401
+    from nbody.lib import (BUILD_QUANTIZED_KEYS, REC_DF, REC_FP64, REC_LEARNED, build_mask_for,
+                           records_for)
+    assert records_for("theta", "f64") == REC_FP64
+    assert records_for("theta", "f64_ieee") == REC_FP64
+    assert records_for("group", "f64") == REC_FP64
+    assert records_for("theta", "df64") == REC_FP64 | REC_DF
+    assert records_for("theta", "f32c") == 0 and records_for("group", "f32c") == 0
+    assert records_for("learned", "f32c") == REC_LEARNED
+    for opening, precision in (("theta", "f64"), ("theta", "df64"), ("group", "f64")):
+        assert not build_mask_for(opening, precision) & BUILD_QUANTIZED_KEYS
+    for opening, precision in (("theta", "f32c"), ("group", "f32c"), ("learned", "f32c")):
+        assert build_mask_for(opening, precision) & BUILD_QUANTIZED_KEYS
