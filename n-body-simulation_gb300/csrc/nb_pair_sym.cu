@@ -277,7 +277,7 @@ pair_sym_kernel(SymPlan S, const typename RecOf<R>::type* __restrict__ src, R ep
             for (int g = 0; g < JT / 32; ++g) {
                 const Rec* G4 = &tile[buf][g * 32];
                 R jx = 0, jy = 0, jz = 0;  // sums of body (lane + s) mod 32 of the group
-#pragma unroll 4
+#pragma unroll 8
                 for (int s = 0; s < 32; ++s) {
                     const Rec J = G4[(lane + s) & 31];
                     R jm;
