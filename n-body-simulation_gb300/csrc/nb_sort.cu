@@ -118,6 +118,7 @@ constexpr uint32_t LB_TOTAL = 2u << 30;
 constexpr uint32_t LB_VALUE = (1u << 30) - 1u;
 constexpr unsigned long long LB_WAIT_LIMIT = 1ull << 22;
 constexpr int LB_WINDOW = 8;  // predecessor words read per look-back round trip
+static_assert(RS_THREADS == RS_BINS, "the look-back and the digit scan run one thread per digit");
 
 // hist[p][d]: keys whose digit of pass p is d, for all passes in one read.
 __global__ void __launch_bounds__(RS_THREADS)
@@ -307,6 +308,8 @@ nb_status radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
                            void* temp, uint32_t* err, cudaStream_t stream, int* result_in_alt) {
     *result_in_alt = 0;
     if (n <= 1) return NB_OK;
+    if (n > LB_VALUE)  // look-back words count keys in 30 bits
+        return set_error(NB_ERR_INVALID_ARG, "radix_sort_pairs: n = %u above 2^30 - 1", n);
     const int passes = (end_bit - begin_bit + 7) / 8;
     if (passes < 1 || passes > RS_MAX_PASSES)
         return set_error(NB_ERR_INVALID_ARG, "radix_sort_pairs: bit range [%d, %d)", begin_bit,
