@@ -121,6 +121,16 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
+def headline_config(ws: int) -> dict:
+    """The workload both arms (ours and --impl reference) report, as one dict."""
+    return {"workload": f"barnes-hut fp64 theta={THETA}, {N_BODIES:,}-body heliocentric disc "
+                        f"(seed {SEED}), dt=1h, per-body opening rule (the reference's), "
+                        "leapfrog + build + traversal per step",
+            "bodies": N_BODIES, "theta": THETA, "dt_days": DT, "eps2": EPS2,
+            "l2": "GPU arm: 256 MB buffer written before every timed step (L2 is 129 MB)",
+            "parallelism": f"replicas x{ws}"}
+
+
 # ---------------------------------------------------------------------------------------------
 # CPU baseline (the oracle: C++/OpenMP restatement of the reference, timed on the host cores)
 # ---------------------------------------------------------------------------------------------
@@ -217,14 +227,14 @@ def run_reference(args):
     t_step = sum(times) / len(times)
     value = 1.0 / t_step
     sample = (f"each step: leapfrog + full octree build of {N_BODIES} bodies + traversal of "
-              f"1/{int(round(1 / frac))} of the bodies (strided) scaled to all bodies")
+              f"1/{int(round(1 / frac))} of the bodies (strided) scaled to all bodies; every "
+              f"step starts from the initial state (not advanced between timed steps) with zero "
+              f"accelerations in its leapfrog")
     line = {"impl": "reference", "metric": "bh_steps_per_s_1M_fp64_theta0.5", "value": value,
             "unit": "steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "barnes-hut fp64 theta=0.5, 1,048,576-body heliocentric disc, "
-                                   "dt=1h, per-body opening rule",
-                       "bodies": N_BODIES, "theta": THETA},
+            "config": headline_config(ws),
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0,
@@ -391,12 +401,7 @@ def run_ours(args):
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "barnes-hut fp64 theta=0.5, 1,048,576-body heliocentric disc, "
-                                   "dt=1h, per-body opening rule (the reference's), "
-                                   "leapfrog + build + traversal per step",
-                       "bodies": n, "theta": THETA, "dt_days": DT, "eps2": EPS2,
-                       "l2": "256 MB buffer written before every timed step",
-                       "parallelism": f"replicas x{ws}"},
+            "config": headline_config(ws),
             "e2e": {"value": e2e_value, "unit": "steps/s",
                     "h2d_bytes_per_step": 8 * n * len(h2d_arrays),
                     "d2h_bytes_per_step": 8 * n * 9},
@@ -539,6 +544,136 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
     return out
 
 
+# ---------------------------------------------------------------------------------------------
+# profiling cases (--case): small, self-contained runs of single kernels for ncu captures
+# ---------------------------------------------------------------------------------------------
+def pair_case(n: int = 262144, config: int = 0, symmetric: bool = False):
+    import torch
+
+    from nbody import generators, learned
+    from nbody.lib import (SYM_ALWAYS, SYM_NEVER, Context, set_naive_pair_config,
+                           set_naive_symmetric)
+    ctx = Context(0)
+    if symmetric:
+        set_naive_symmetric(SYM_ALWAYS, config)
+    else:
+        set_naive_symmetric(SYM_NEVER, 0)
+        set_naive_pair_config(config)
+    t = learned.device_system(generators.plummer(n, 1))
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    for _ in range(3):
+        ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, 1.0, 1e-6, "f32c")
+    ctx.sync()
+
+
+def sym64_case(n: int = 65536, config: int = 0):
+    import torch
+
+    from nbody import generators, learned
+    from nbody.lib import SYM_ALWAYS, Context, set_naive_symmetric
+    ctx = Context(0)
+    set_naive_symmetric(SYM_ALWAYS, 0, config)
+    d = generators.heliocentric_disc(n, 1)
+    t = learned.device_system(d)
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    for _ in range(3):
+        ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, d["G"], learned.EPS2, "f64")
+    ctx.sync()
+
+
+def learned_case(n: int = 262144, log10_tau: float = -4.25, pairs: int = 2_000_000):
+    import torch
+
+    from nbody import generators, learned
+    from nbody.lib import BHTree, Context
+    ctx = Context(0)
+    X, Y = learned.training_set(ctx, n, pairs)
+    params, _ = learned.train(ctx, X, Y, epochs=4)
+    d = generators.disc_plummer_mix(n, seed=21)
+    t = learned.device_system(d)
+    tree = BHTree(ctx, n, theta=0.4)
+    tree.build(t["m"], t["x"], t["y"], t["z"], d["G"])
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    tree.accel(t["x"], t["y"], t["z"], *acc, d["G"], learned.EPS2, "group", "f32c")
+    tree.set_policy(params, log10_tau, 0.3, learned.NO_CAP)
+    for _ in range(3):
+        tree.accel(t["x"], t["y"], t["z"], *acc, d["G"], learned.EPS2, "learned", "f32c")
+    ctx.sync()
+
+
+def df64_case(n: int = 262144):
+    import torch
+
+    from nbody import generators, learned
+    from nbody.lib import BHTree, Context
+    ctx = Context(0)
+    d = generators.heliocentric_disc(n, 1)
+    t = learned.device_system(d)
+    tree = BHTree(ctx, n, theta=0.5)
+    tree.build(t["m"], t["x"], t["y"], t["z"], d["G"])
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    for _ in range(3):
+        tree.accel(t["x"], t["y"], t["z"], *acc, d["G"], learned.EPS2, "theta", "df64")
+    ctx.naive_accel(t["m"], t["x"], t["y"], t["z"], *acc, d["G"], learned.EPS2, "df64")
+    ctx.sync()
+
+
+def batch_case(systems: int = 512, config: int = -1):
+    """The 512-system Plummer ensemble (N log-uniform in [256, 16384], seed 3): batch pair
+    kernel in tile configuration `config` (-1: the autotuner's choice), three evaluations."""
+    import numpy as np
+    import torch
+
+    from nbody import generators, learned, workloads
+    from nbody.lib import Batch, Context
+    ctx = Context(0)
+    counts = workloads._ensemble_counts(systems, 256, 16384, 3)
+    parts = [generators.plummer(int(c), seed=3 * 100003 + s) for s, c in enumerate(counts)]
+    cat = {k: np.concatenate([p[k] for p in parts]) for k in ("m", "x", "y", "z", "vx", "vy", "vz")}
+    t = learned.device_system(cat)
+    n = len(cat["m"])
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    b = Batch(ctx, counts)
+    if config < 0:
+        b.autotune(t["m"], t["x"], t["y"], t["z"], *acc, 1.0, 1e-6, reps=2)
+    else:
+        b.set_config(config)
+    for _ in range(3):
+        b.accel(t["m"], t["x"], t["y"], t["z"], *acc, 1.0, 1e-6)
+    ctx.sync()
+    b.close()
+
+
+def build_case(n: int = 1 << 20, mask: str = "fp64"):
+    """Three octree builds of the seeded heliocentric disc with the node record set of a
+    traversal: "fp64" (the headline's), "learned" (learned policy, quantized keys) or "all"."""
+    from nbody import generators, learned
+    from nbody.lib import BUILD_QUANTIZED_KEYS, REC_ALL, REC_FP64, REC_LEARNED, BHTree, Context
+    masks = {"fp64": REC_FP64, "learned": REC_LEARNED | BUILD_QUANTIZED_KEYS, "all": REC_ALL}
+    ctx = Context(0)
+    d = generators.heliocentric_disc(n, 1)
+    t = learned.device_system(d)
+    tree = BHTree(ctx, n, theta=0.5)
+    tree.set_records(masks[mask])
+    for _ in range(3):
+        tree.build(t["m"], t["x"], t["y"], t["z"], d["G"])
+    ctx.sync()
+    tree.close()
+
+
+CASES = {
+    "pair": lambda a: pair_case(int(a[0]) if a else 262144, int(a[1]) if len(a) > 1 else 0),
+    "sym": lambda a: pair_case(int(a[0]) if a else 262144, int(a[1]) if len(a) > 1 else 0, True),
+    "sym64": lambda a: sym64_case(int(a[0]) if a else 65536, int(a[1]) if len(a) > 1 else 0),
+    "learned": lambda a: learned_case(int(a[0]) if a else 262144,
+                                      float(a[1]) if len(a) > 1 else -4.25,
+                                      int(a[2]) if len(a) > 2 else 2_000_000),
+    "df64": lambda a: df64_case(int(a[0]) if a else 262144),
+    "batch": lambda a: batch_case(int(a[0]) if a else 512, int(a[1]) if len(a) > 1 else -1),
+    "build": lambda a: build_case(int(a[0]) if a else 1 << 20, a[1] if len(a) > 1 else "fp64"),
+}
+
+
 def main():
     global N_BODIES
     ap = argparse.ArgumentParser()
@@ -550,7 +685,17 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the secondary measurements")
     ap.add_argument("--bodies", type=int, default=N_BODIES,
                     help="bodies of the disc (default 1,048,576; smaller only for profiling)")
+    ap.add_argument("--case", nargs="+", metavar=("NAME", "ARG"),
+                    help="run one profiling case instead of the benchmark: pair [N] [config], "
+                         "sym [N] [config], sym64 [N] [config], learned [N] [log10_tau] [pairs], "
+                         "df64 [N], batch [systems] [config], build [N] [fp64|learned|all]")
     args = ap.parse_args()
+    if args.case:
+        if args.case[0] not in CASES:
+            ap.error(f"unknown case {args.case[0]!r}; one of {', '.join(CASES)}")
+        CASES[args.case[0]](args.case[1:])
+        print("ok")
+        return 0
     if args.warmup < 3:
         args.warmup = 3
     N_BODIES = args.bodies

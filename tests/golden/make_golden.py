@@ -108,5 +108,7 @@ def main(ref_root: str, out_path: str):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    main(root, os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <root of the reference checkout>")
+    main(sys.argv[1], os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                                   "reference_kats.json"))
