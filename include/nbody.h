@@ -66,6 +66,30 @@ nb_status nb_sync(nb_ctx* ctx, nb_stream_t stream);
 const char* nb_last_error_string(void);
 const char* nb_version(void);
 
+/* Failure-path hooks for tests (no reference counterpart: the reference's device waits and its
+ * traversal stack are unchecked, BarnesHutOctree.cpp:263-384, BarnesHutAlgorithm.cpp:340-388).
+ * They act on later launches of this context only and make a failure happen without faulting
+ * the GPU:
+ *  - wait_limit: polls of every bounded device-side wait before it gives up and sets the
+ *    timeout bit (nb_sync then returns NB_ERR_TIMEOUT); negative = the default (2^22); 0 = no
+ *    waiting at all (a tile wait gives up without polling, a look-back gives up at the first
+ *    count not yet published). Honoured by the pair kernels' tile waits (nb_naive_accel,
+ *    nb_naive_accel_range, nb_batch_naive_accel) and the radix look-back of
+ *    nb_util_radix_sort_pairs; the octree build keeps the default. A CTA
+ *    whose wait ran out still drains its own copies in flight with the default limit before it
+ *    leaves (should that drain run out too, nb_sync reports it and the context refuses all
+ *    further calls, since copies may still land in shared memory after the CTA left).
+ *  - flags NB_FAULT_DROP_LOOKBACK: nb_util_radix_sort_pairs drops the first tile's published
+ *    count in every digit pass, so later tiles wait for a word that nothing writes.
+ *  - learned_stack_cap: cells the NB_OPEN_LEARNED traversal's per-warp stack may hold, 1 ..
+ *    NB_LEARNED_STACK_CAP (0 = all); a walk that would exceed it stops and sets the stack bit
+ *    (nb_sync returns NB_ERR_STACK_OVERFLOW).
+ * Results of a launch that hit a limit are undefined; the context stays usable. */
+#define NB_FAULT_DROP_LOOKBACK 1u
+#define NB_LEARNED_STACK_CAP 1024u
+nb_status nb_ctx_set_fault_hooks(nb_ctx* ctx, long long wait_limit, unsigned int flags,
+                                 unsigned int learned_stack_cap);
+
 /* ---------------------------------------------------------------------------------------------
  * Naive all-pairs acceleration.
  * Replaces NaiveAlgorithm::computeAccelerations_opt_{0,1,2} (NaiveAlgorithm.hpp:31-53,
@@ -194,9 +218,15 @@ nb_status nb_energy(nb_ctx* ctx, const double* m, const double* x, const double*
  * file-scope device array, present on every GPU that loads the library until the process exits.
  * Limit: n <= NB_ENERGY_NOALLOC_MAX_N bodies (larger n returns NB_ERR_INVALID_ARG).
  * Runs on the current device. Its first call on each device looks up that array's device
- * address (cudaGetSymbolAddress); make that first call before any stream capture. All calls
- * share the array: calls that overlap on the GPU race, so serialise them (one stream at a
- * time). out_dev: DEVICE pointer to 4 doubles {kinetic, potential, total, virial}. */
+ * address (cudaGetSymbolAddress); with CUDA's lazy module loading that lookup is also what loads
+ * the library's device code on that device, and loading it is when the driver allocates the
+ * fixed array. So make one call per device during initialisation, before any stream capture and
+ * before the caller's memory pool takes the device's memory; later calls allocate nothing. The
+ * address is kept for the life of the process: a cudaDeviceReset (or anything else that tears
+ * down the device's primary context) invalidates it, and the entry point must not be called on
+ * that device afterwards. All calls share the array: calls that overlap on the GPU race, so
+ * serialise them (one stream at a time). out_dev: DEVICE pointer to 4 doubles {kinetic,
+ * potential, total, virial}. */
 #define NB_ENERGY_NOALLOC_MAX_N 1048576u
 nb_status nb_energy_noalloc(const double* m, const double* x, const double* y, const double* z,
                             const double* vx, const double* vy, const double* vz, uint32_t n,
@@ -404,6 +434,17 @@ nb_status nb_bh_generate_pairs(nb_ctx* ctx, const nb_bh_tree* tree, const double
 #define NB_POLICY_BOUND_ACCEPT 1u
 nb_status nb_bh_set_policy(nb_bh_tree* tree, const float* params_dev, float log10_tau,
                            double theta_fallback, uint32_t count_cap, uint32_t flags);
+/* Opening-policy files (host-side, synchronous): a trained network (NB_MLP_PARAMS FP32 values in
+ * HOST memory, the layout above) with the nb_bh_set_policy settings it was tuned for. Text
+ * format, one item per line: "nbody-gb300 opening policy 1", "network 8 32 32 1 relu",
+ * "log10_tau <v>", "theta_fallback <v>", "count_cap <v>", "flags <v>", "params 1377", then the
+ * 1377 parameters (9 significant digits: FP32 values round-trip exactly). nb_policy_load rejects
+ * any other shape or a malformed file with NB_ERR_INVALID_ARG. The host driver reads these files
+ * (nbody_sim --opening=learned --policy=<file>). */
+nb_status nb_policy_save(const char* path, const float* params_host, float log10_tau,
+                         double theta_fallback, uint32_t count_cap, uint32_t flags);
+nb_status nb_policy_load(const char* path, float* params_host, float* log10_tau,
+                         double* theta_fallback, uint32_t* count_cap, uint32_t* flags);
 /* NB_OPEN_LEARNED traversal that also counts, into 4 DEVICE uint64: body-cell interactions
  * (counters_dev[0]), cells decided by the policy (network, or theta rule when the policy has no
  * network) ([1]), cells visited ([2]) and walk steps of up to 32 cells ([3]), summed over

@@ -103,13 +103,17 @@ nb_status apply_config(nb_batch* b, int cfg, int sm_count) {
 nb_status batch_accel(nb_ctx* ctx, nb_batch* b, const double* m, const double* x, const double* y,
                       const double* z, double* ax, double* ay, double* az, double G, double eps2,
                       cudaStream_t s) {
-    if (is_sym(b->cfg))
-        return nb::sym_launch(nb::SYM_F32, b->cfg - nb::NB_PAIR_CONFIGS, b->sym_plan, m, x, y,
-                              z, G, eps2,
+    if (is_sym(b->cfg)) {
+        nbsym::SymPlan S = b->sym_plan;
+        S.wait_limit = ctx->wait_limit;
+        return nb::sym_launch(nb::SYM_F32, b->cfg - nb::NB_PAIR_CONFIGS, S, m, x, y, z, G, eps2,
                               b->sym_src, b->sym_part_i, b->sym_part_j, ax, ay, az,
                               ctx->dev_error, s);
+    }
     if (b->plan.units == 0) return NB_OK;
-    return nb::pair_launch(b->cfg, b->plan, m, x, y, z, b->n_total, b->n_total, G, eps2, b->src,
+    nbpair::Plan P = b->plan;
+    P.wait_limit = ctx->wait_limit;
+    return nb::pair_launch(b->cfg, P, m, x, y, z, b->n_total, b->n_total, G, eps2, b->src,
                            b->tgt, b->part, ax, ay, az, ctx->dev_error, s);
 }
 

@@ -93,6 +93,22 @@ nb_status nb_ctx_destroy(nb_ctx* ctx) {
     return NB_OK;
 }
 
+nb_status nb_ctx_set_fault_hooks(nb_ctx* ctx, long long wait_limit, unsigned int flags,
+                                 unsigned int learned_stack_cap) {
+    NB_CHECK_CTX(ctx);
+    if (flags & ~(unsigned int)NB_FAULT_DROP_LOOKBACK)
+        return nb::set_error(NB_ERR_INVALID_ARG, "nb_ctx_set_fault_hooks: unknown flags 0x%x",
+                             flags);
+    if (learned_stack_cap > NB_LEARNED_STACK_CAP)
+        return nb::set_error(NB_ERR_INVALID_ARG,
+                             "nb_ctx_set_fault_hooks: stack capacity %u above the kernel's %u",
+                             learned_stack_cap, (unsigned)NB_LEARNED_STACK_CAP);
+    ctx->wait_limit = wait_limit < 0 ? NB_WAIT_LIMIT_DEFAULT : (unsigned long long)wait_limit;
+    ctx->fault_flags = flags;
+    ctx->learned_stack_cap = learned_stack_cap;
+    return NB_OK;
+}
+
 nb_status nb_sync(nb_ctx* ctx, nb_stream_t stream) {
     NB_CHECK_CTX(ctx);
     NB_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
@@ -100,6 +116,12 @@ nb_status nb_sync(nb_ctx* ctx, nb_stream_t stream) {
     NB_CUDA_TRY(cudaMemcpy(&word, ctx->dev_error, sizeof(word), cudaMemcpyDeviceToHost));
     if (word) {
         NB_CUDA_TRY(cudaMemset(ctx->dev_error, 0, sizeof(word)));
+        if (word & NB_DEVERR_DRAIN) {
+            ctx->unusable = true;
+            return nb::set_error(NB_ERR_TIMEOUT,
+                                 "device: a bounded wait ran out and its CTA could not drain its "
+                                 "bulk copies in flight; the context refuses further work");
+        }
         if (word & NB_DEVERR_POOL)
             return nb::set_error(NB_ERR_POOL_OVERFLOW, "device: octree node pool overflow");
         if (word & NB_DEVERR_DEPTH)

@@ -15,7 +15,15 @@ enum : uint32_t {
     NB_DEVERR_DEPTH = 1u << 1,
     NB_DEVERR_STACK = 1u << 2,
     NB_DEVERR_TIMEOUT = 1u << 3,
+    // a CTA whose wait ran out could not drain its own bulk copies in flight either and left
+    // with them outstanding: the launch's memory state is undefined, the context refuses work
+    NB_DEVERR_DRAIN = 1u << 4,
 };
+
+// Iterations of a bounded device-side wait (mbarrier polls, look-back polls) before it gives
+// up. A context can lower it for the failure-path tests (nb_ctx_set_fault_hooks); the waits
+// that drain a CTA's own copies in flight before it leaves always use this default.
+constexpr unsigned long long NB_WAIT_LIMIT_DEFAULT = 1ull << 22;
 
 struct nb_scratch_buf {
     void* ptr = nullptr;
@@ -49,6 +57,12 @@ struct nb_ctx {
     uint32_t* dev_error = nullptr;  // device error word (NB_DEVERR_* bits)
     unsigned int* dev_counter = nullptr;  // last-block-done counters for fused grid reductions
     nb_scratch_buf scratch[NB_SCRATCH_COUNT];
+    // failure-path test hooks (nb_ctx_set_fault_hooks)
+    unsigned long long wait_limit = NB_WAIT_LIMIT_DEFAULT;
+    unsigned int fault_flags = 0;
+    unsigned int learned_stack_cap = 0;  // 0 = the kernel's full capacity
+    // set when a launch left bulk copies outstanding (NB_DEVERR_DRAIN): every later call fails
+    bool unusable = false;
 };
 
 namespace nb {
@@ -66,6 +80,11 @@ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 #define NB_CHECK_CTX(ctx)                                                                  \
     do {                                                                                   \
         if (!(ctx)) return nb::set_error(NB_ERR_INVALID_ARG, "%s: null context", __func__); \
+        if ((ctx)->unusable)                                                               \
+            return nb::set_error(NB_ERR_TIMEOUT,                                           \
+                                 "%s: context unusable after a launch left copies in "    \
+                                 "flight; destroy it",                                     \
+                                 __func__);                                                \
     } while (0)
 
 #define NB_TRY(expr)                     \

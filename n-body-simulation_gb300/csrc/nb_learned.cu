@@ -310,7 +310,7 @@ __device__ float mlp32(const __nv_bfloat16* __restrict__ feat, int lane, const F
 // ---------------------------------------------------------------------------------------------
 constexpr int LT_WARPS = 4;
 constexpr int LT_THREADS = LT_WARPS * 32;
-constexpr int LT_CAP = 1024;        // stack entries per warp
+constexpr int LT_CAP = (int)NB_LEARNED_STACK_CAP;  // stack entries per warp
 constexpr int LT_RESERVE = 7 * NB_MAX_TREE_DEPTH + 8;  // headroom of single-cell steps
 constexpr int LT_BATCH = 32;        // cells popped per step (one per lane)
 constexpr uint32_t LT_DIRECT = 8;   // opened cells up to this many bodies: direct sums
@@ -368,7 +368,8 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
                   float theta2, uint32_t count_cap, float eps2, const uint32_t* __restrict__ ids,
                   double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az,
                   unsigned long long* __restrict__ counters, uint32_t* __restrict__ err_word,
-                  uint32_t* __restrict__ next_group) {
+                  uint32_t* __restrict__ next_group, int cap) {
+    // cap <= LT_CAP: the stack entries a walk may use (LT_CAP except in the failure-path tests)
     __shared__ uint32_t stack[LT_WARPS][LT_CAP];
     __shared__ __align__(16) __nv_bfloat16 feat[LT_WARPS][LT_BATCH][16];
     // the group's positions as packed pairs (bodies 2j, 2j+1) per axis, for the gap loop
@@ -424,13 +425,14 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
         NodeRec32 r{};
         NodeAux xa{};
         uint4 c0, c1;
-        // Pops the next step's cells and issues their loads. Wide steps keep top <= LT_CAP -
+        // Pops the next step's cells and issues their loads. Wide steps keep top <= cap -
         // LT_RESERVE; single-cell steps are a plain depth-first walk, which adds at most 7 entries
-        // per tree level, so they stay below LT_CAP.
+        // per tree level, so with cap = LT_CAP they stay below it. A step whose pushes could pass
+        // cap (only with a smaller cap) is not taken: the walk stops with the stack bit.
         auto pop_and_load = [&]() -> int {
             __syncwarp();
-            int nb = top > 0 ? min(min(LT_BATCH, top), max(1, (LT_CAP - LT_RESERVE - top) / 7)) : 0;
-            if (nb > 0 && top + 7 * nb > LT_CAP) {  // unreachable by the bound above; report, stop
+            int nb = top > 0 ? min(min(LT_BATCH, top), max(1, (cap - LT_RESERVE - top) / 7)) : 0;
+            if (nb > 0 && top + 7 * nb > cap) {  // unreachable for cap = LT_CAP; report, stop
                 if (lane == 0) atomicOr(err_word, NB_DEVERR_STACK);
                 nb = 0;
             }
@@ -1014,7 +1016,8 @@ nb_status launch_learned(nb_ctx* ctx, const nb_bh_tree* t, const double* x, cons
         t->policy_log_tau * 0.2f,
         (t->policy_flags & NB_POLICY_BOUND_ACCEPT) ? exp10f(t->policy_log_tau) : 0.f,
         t->policy_theta * t->policy_theta, t->policy_count_cap,
-        (float)eps2, t->ids, ax, ay, az, counters, ctx->dev_error, t->work);
+        (float)eps2, t->ids, ax, ay, az, counters, ctx->dev_error, t->work,
+        ctx->learned_stack_cap ? (int)ctx->learned_stack_cap : LT_CAP);
     return check_launch("bh_learned_kernel");
 }
 

@@ -192,8 +192,9 @@ int g_naive_sym_mode = 1;
 int g_naive_sym_cfg[3] = {0, 0, 0};
 // Automatic selection wants at least this many units per persistent CTA (the one-sided kernels
 // spread small systems better) and j-side partials (3 values per unit and tile body) below the
-// cap.
-constexpr uint64_t SYM_MIN_UNITS_PER_CTA = 8;
+// cap. With 7, a 16,384-body system takes the FP64 shape (4,2,64) at its 7 resident CTAs per SM
+// (8,320 units over 1,064 CTAs) and the larger (4,4,64) I-block from ~18,000 bodies on.
+constexpr uint64_t SYM_MIN_UNITS_PER_CTA = 7;
 constexpr size_t SYM_PART_CAP_BYTES = (size_t)4 << 30;
 
 // Runs the symmetric kernel of arithmetic form `form` (nb::SymForm) for the whole system when
@@ -246,6 +247,7 @@ nb_status naive_sym(nb_ctx* ctx, int form, const double* m, const double* x, con
     S.n_total = hp.n_total;
     S.n_records = hp.n_records;
     S.units = hp.units;
+    S.wait_limit = ctx->wait_limit;
     b += table_bytes;
     *done = true;
     return nb::sym_launch(form, cfg, S, m, x, y, z, G, eps2, b, b + src_bytes,
@@ -300,6 +302,7 @@ nb_status naive_f32c(nb_ctx* ctx, const double* m, const double* x, const double
     P.t_off = t_off;
     P.unit_off = unit_off;
     P.ib_off = ib_off;
+    P.wait_limit = ctx->wait_limit;
     return nb::pair_launch(cfg, P, m, x, y, z, n, n_t, G, eps2, src, tgt, part, ax, ay, az,
                            ctx->dev_error, stream);
 }

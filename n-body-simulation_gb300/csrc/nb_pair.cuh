@@ -28,6 +28,7 @@ struct Plan {
     uint32_t n_systems;
     uint32_t ctas;
     uint64_t units;
+    unsigned long long wait_limit;  // polls of a tile wait before it gives up (context's limit)
     const uint32_t* sys_off;    // [n_systems+1] first source body of each system
     const uint32_t* tgt_begin;  // [n_systems]   first target (relative to the system)
     const uint32_t* t_off;      // [n_systems+1] prefix of target counts
@@ -35,7 +36,6 @@ struct Plan {
     const uint32_t* ib_off;     // [n_systems+1] prefix of i-blocks
 };
 
-constexpr unsigned long long WAIT_LIMIT = 1ull << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -56,8 +56,10 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
         "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (unsigned long long it = 0; it < WAIT_LIMIT; ++it) {
+// Polls the mbarrier phase at most `limit` times; false when it has not completed by then.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          unsigned long long limit) {
+    for (unsigned long long it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -205,7 +207,7 @@ pair_f32c_kernel(Plan P, const SrcDup* __restrict__ src, const float4* __restric
         for (; u < seg_end; ++u, ++iter, ++jt) {
             const int buf = iter & 1;
             const uint32_t cnt = min((uint32_t)JT, w.n_src - jt * JT);
-            const bool ok = mbar_wait(&full[buf], (iter >> 1) & 1);
+            const bool ok = mbar_wait(&full[buf], (iter >> 1) & 1, P.wait_limit);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
@@ -253,8 +255,12 @@ pair_f32c_kernel(Plan P, const SrcDup* __restrict__ src, const float4* __restric
             for (int c = 0; c < 6; ++c) out[c * IB + k * THREADS + th] = hl[c][k][th];
     }
     if (failed) {
-        if (threadIdx.x == 0) atomicOr(err_word, NB_DEVERR_TIMEOUT);
-        for (uint32_t k = iter; k < iter + 2 && u0 + k < u1; ++k) mbar_wait(&full[k & 1], (k >> 1) & 1);
+        // the copies of units iter and iter + 1 were issued: wait for them (default limit)
+        // before the CTA leaves, so that none lands in shared memory after it
+        bool drained = true;
+        for (uint32_t k = iter; k < iter + 2 && u0 + k < u1; ++k)
+            drained &= mbar_wait(&full[k & 1], (k >> 1) & 1, NB_WAIT_LIMIT_DEFAULT);
+        if (threadIdx.x == 0) atomicOr(err_word, NB_DEVERR_TIMEOUT | (drained ? 0u : NB_DEVERR_DRAIN));
     }
 }
 

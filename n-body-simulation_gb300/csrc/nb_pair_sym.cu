@@ -264,7 +264,7 @@ pair_sym_kernel(SymPlan S, const typename RecOf<R>::type* __restrict__ src, R ep
         }
         for (; u < seg_end; ++u, ++iter, ++jt) {
             const int buf = iter & 1;
-            const bool ok = mbar_wait(&full[buf], (iter >> 1) & 1);
+            const bool ok = mbar_wait(&full[buf], (iter >> 1) & 1, S.wait_limit);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
@@ -359,10 +359,12 @@ pair_sym_kernel(SymPlan S, const typename RecOf<R>::type* __restrict__ src, R ep
                 for (int c = 0; c < 6; ++c) out[c * IB + k * 32] = hl[c][k][th];
         }
     }
-    if (failed) {
-        if (threadIdx.x == 0) atomicOr(err_word, NB_DEVERR_TIMEOUT);
+    if (failed) {  // drain the copies of units iter, iter + 1 before leaving (default limit)
+        bool drained = true;
         for (uint32_t k = iter; k < iter + 2 && u0 + k < u1; ++k)
-            mbar_wait(&full[k & 1], (k >> 1) & 1);
+            drained &= mbar_wait(&full[k & 1], (k >> 1) & 1, NB_WAIT_LIMIT_DEFAULT);
+        if (threadIdx.x == 0)
+            atomicOr(err_word, NB_DEVERR_TIMEOUT | (drained ? 0u : NB_DEVERR_DRAIN));
     }
 }
 
@@ -432,7 +434,7 @@ pair_sym_df_kernel(SymPlan S, const RecTF* __restrict__ src, float e2h, float e2
         }
         for (; u < seg_end; ++u, ++iter, ++jt) {
             const int buf = iter & 1;
-            const bool ok = mbar_wait(&full[buf], (iter >> 1) & 1);
+            const bool ok = mbar_wait(&full[buf], (iter >> 1) & 1, S.wait_limit);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
@@ -543,10 +545,12 @@ pair_sym_df_kernel(SymPlan S, const RecTF* __restrict__ src, float e2h, float e2
             out[2 * IB + k * 32] = tz[k];
         }
     }
-    if (failed) {
-        if (threadIdx.x == 0) atomicOr(err_word, NB_DEVERR_TIMEOUT);
+    if (failed) {  // drain the copies of units iter, iter + 1 before leaving (default limit)
+        bool drained = true;
         for (uint32_t k = iter; k < iter + 2 && u0 + k < u1; ++k)
-            mbar_wait(&full[k & 1], (k >> 1) & 1);
+            drained &= mbar_wait(&full[k & 1], (k >> 1) & 1, NB_WAIT_LIMIT_DEFAULT);
+        if (threadIdx.x == 0)
+            atomicOr(err_word, NB_DEVERR_TIMEOUT | (drained ? 0u : NB_DEVERR_DRAIN));
     }
 }
 

@@ -20,6 +20,7 @@ struct SymPlan {
     const SymSys* sys;  // device, n_systems + 1 entries
     uint32_t n_systems, ctas, n_total, n_records;
     uint64_t units;
+    unsigned long long wait_limit;  // polls of a tile wait before it gives up (context's limit)
 };
 
 // First unit of I-block a of a system with n_jt j-tiles (row a holds the j-tiles a * tpb ..

@@ -116,7 +116,6 @@ constexpr int RS_MAX_PASSES = 8;
 constexpr uint32_t LB_AGGREGATE = 1u << 30;
 constexpr uint32_t LB_TOTAL = 2u << 30;
 constexpr uint32_t LB_VALUE = (1u << 30) - 1u;
-constexpr unsigned long long LB_WAIT_LIMIT = 1ull << 22;
 constexpr int LB_WINDOW = 8;  // predecessor words read per look-back round trip
 static_assert(RS_THREADS == RS_BINS, "the look-back and the digit scan run one thread per digit");
 
@@ -163,7 +162,8 @@ __global__ void __launch_bounds__(RS_THREADS)
 radix_pass_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                   uint64_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
                   int shift, const uint32_t* __restrict__ digit_off, uint32_t* __restrict__ lb,
-                  uint32_t* __restrict__ ticket, uint32_t* __restrict__ err) {
+                  uint32_t* __restrict__ ticket, uint32_t* __restrict__ err,
+                  unsigned long long wait_limit, int drop_first) {
     __shared__ uint32_t wcnt[RS_WARPS][RS_BINS];
     __shared__ uint32_t tile_base[RS_BINS];   // first output position of the tile's digit d
     __shared__ uint32_t digit_local[RS_BINS];  // first tile position of digit d after the reorder
@@ -209,7 +209,9 @@ radix_pass_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restri
         uint32_t* mine = lb + (size_t)tile * RS_BINS + d;
         uint32_t before = 0;
         if (tile == 0) {
-            lb_store(mine, LB_TOTAL | run);
+            // drop_first (failure-path test hook): the first tile's count is never published,
+            // so the tiles after it wait for a word that nothing writes
+            if (!drop_first) lb_store(mine, LB_TOTAL | run);
         } else {
             lb_store(mine, LB_AGGREGATE | run);
             // walk back in windows of LB_WINDOW predecessors, their words loaded together (one
@@ -225,7 +227,7 @@ radix_pass_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restri
                     if (done || t0 - j < 0) break;
                     const uint32_t* w = lb + (size_t)(t0 - j) * RS_BINS + d;
                     for (unsigned long long it = 0; (v[j] & (LB_AGGREGATE | LB_TOTAL)) == 0; ++it) {
-                        if (it >= LB_WAIT_LIMIT) {
+                        if (it >= wait_limit) {
                             timed_out = true;
                             break;
                         }
@@ -305,7 +307,8 @@ size_t radix_temp_bytes(uint32_t n) {
 
 nb_status radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
                            uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit,
-                           void* temp, uint32_t* err, cudaStream_t stream, int* result_in_alt) {
+                           void* temp, uint32_t* err, cudaStream_t stream, int* result_in_alt,
+                           unsigned long long wait_limit, int drop_first) {
     *result_in_alt = 0;
     if (n <= 1) return NB_OK;
     if (n > LB_VALUE)  // look-back words count keys in 30 bits
@@ -332,7 +335,7 @@ nb_status radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
     for (int p = 0; p < passes; ++p) {
         radix_pass_kernel<<<tiles, RS_THREADS, 0, stream>>>(
             kin, vin, kout, vout, n, begin_bit + 8 * p, offs + p * RS_BINS,
-            lb + (size_t)p * tiles * RS_BINS, tickets + p, err);
+            lb + (size_t)p * tiles * RS_BINS, tickets + p, err, wait_limit, drop_first);
         NB_TRY(check_launch("radix_pass_kernel"));
         uint64_t* tk = kin;
         kin = kout;
@@ -367,7 +370,8 @@ nb_status nb_util_radix_sort_pairs(nb_ctx* ctx, uint64_t* keys, uint32_t* vals, 
     NB_CUDA_TRY(cudaMallocAsync(&tmp, nb::radix_temp_bytes(n), s));
     int in_alt = 0;
     nb_status st = nb::radix_sort_pairs(keys, vals, ka, va, n, begin_bit, end_bit, tmp,
-                                        ctx->dev_error, s, &in_alt);
+                                        ctx->dev_error, s, &in_alt, ctx->wait_limit,
+                                        (ctx->fault_flags & NB_FAULT_DROP_LOOKBACK) ? 1 : 0);
     if (st == NB_OK && in_alt) {
         cudaMemcpyAsync(keys, ka, (size_t)n * 8, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(vals, va, (size_t)n * 4, cudaMemcpyDeviceToDevice, s);

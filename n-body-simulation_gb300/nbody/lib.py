@@ -46,6 +46,7 @@ SIGNATURES = {
     "nb_energy": [_vp] + [_vp] * 7 + [_u32, _d, _vp, _vp],
     "nb_aabb": [_vp] + [_vp] * 3 + [_u32, _vp, _vp],
     "nb_energy_noalloc": [_vp] * 7 + [_u32, _d, _vp, _vp],
+    "nb_ctx_set_fault_hooks": [_vp, C.c_longlong, C.c_uint, C.c_uint],
 }
 STRING_FUNCS = ("nb_last_error_string", "nb_version")
 
@@ -109,6 +110,12 @@ class Context:
             self.close()
         except Exception:
             pass
+
+    def set_fault_hooks(self, wait_limit=-1, flags=0, learned_stack_cap=0):
+        """Failure-path test hooks of later launches (nb_ctx_set_fault_hooks): wait_limit polls
+        before a bounded wait gives up (-1 = default), FAULT_DROP_LOOKBACK, stack capacity of the
+        learned traversal (0 = full)."""
+        check(self.lib.nb_ctx_set_fault_hooks(self.handle, wait_limit, flags, learned_stack_cap))
 
     def sync(self, stream=None):
         check(self.lib.nb_sync(self.handle, stream_ptr(stream)))
@@ -221,6 +228,9 @@ SIGNATURES.update({
     "nb_bh_export_node_ranges": [_vp, _vp, _vp, _vp, _vp],
     "nb_naive_accel_targets": [_vp] + [_vp] * 4 + [_u32, _vp, _u32] + [_vp] * 3 + [_d, _d, _vp],
     "nb_bh_set_policy": [_vp, _vp, C.c_float, _d, _u32, _u32],
+    "nb_policy_save": [C.c_char_p, _vp, C.c_float, _d, _u32, _u32],
+    "nb_policy_load": [C.c_char_p, _vp, C.POINTER(C.c_float), C.POINTER(_d), C.POINTER(_u32),
+                       C.POINTER(_u32)],
     "nb_bh_set_phase_timing": [_vp, _i],
     "nb_bh_set_records": [_vp, C.c_uint],
     "nb_bh_graph_create": [_vp, _vp] + [_vp] * 13 + [_u32, _d, _d, _d, _i, _i, _i, _vp],
@@ -520,6 +530,10 @@ class Graph:
             pass
 
 
+POLICY_BOUND_ACCEPT = 1  # NB_POLICY_BOUND_ACCEPT
+FAULT_DROP_LOOKBACK = 1  # NB_FAULT_DROP_LOOKBACK
+LEARNED_STACK_CAP = 1024  # NB_LEARNED_STACK_CAP
+
 MLP_PARAMS = 1377
 PAIR_CONFIGS = 8  # NB_PAIR_CONFIG_COUNT
 BATCH_CONFIGS = 16  # NB_BATCH_CONFIG_COUNT: the one-sided shapes, then the symmetric ones
@@ -538,3 +552,28 @@ def mlp_adam(ctx, params, m, v, grad, lr, beta1, beta2, eps, step, stream=None):
 def mlp_predict(ctx, params, X, out, bf16=False, stream=None):
     check(load().nb_mlp_predict(ctx.handle, ptr(params), ptr(X), X.shape[0], ptr(out),
                                 1 if bf16 else 0, stream_ptr(stream)))
+
+
+def policy_save(path, params, log10_tau, theta_fallback, count_cap, flags):
+    """Writes an opening-policy file (nb_policy_save) from a network (any array-like of
+    MLP_PARAMS values, device or host) and its nb_bh_set_policy settings."""
+    import numpy as np
+    if hasattr(params, "detach"):
+        params = params.detach().cpu().numpy()
+    host = np.ascontiguousarray(params, dtype=np.float32)
+    if host.size != MLP_PARAMS:
+        raise ValueError(f"a network has {MLP_PARAMS} parameters, got {host.size}")
+    check(load().nb_policy_save(os.fsencode(path), host.ctypes.data, log10_tau, theta_fallback,
+                                count_cap, flags))
+
+
+def policy_load(path):
+    """(params as a float32 numpy array, log10_tau, theta_fallback, count_cap, flags) of an
+    opening-policy file (nb_policy_load)."""
+    import numpy as np
+    host = np.zeros(MLP_PARAMS, dtype=np.float32)
+    tau, theta = C.c_float(0), C.c_double(0)
+    cap, flags = C.c_uint32(0), C.c_uint32(0)
+    check(load().nb_policy_load(os.fsencode(path), host.ctypes.data, C.byref(tau),
+                                C.byref(theta), C.byref(cap), C.byref(flags)))
+    return host, tau.value, theta.value, cap.value, flags.value

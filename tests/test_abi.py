@@ -70,7 +70,10 @@ def test_python_constants_match_the_header():
     pairs = {"NB_PAIR_CONFIG_COUNT": lib.PAIR_CONFIGS, "NB_BATCH_CONFIG_COUNT": lib.BATCH_CONFIGS,
              "NB_REC_FP64": lib.REC_FP64, "NB_REC_DF": lib.REC_DF,
              "NB_REC_LEARNED": lib.REC_LEARNED, "NB_REC_ALL": lib.REC_ALL,
-             "NB_BUILD_QUANTIZED_KEYS": lib.BUILD_QUANTIZED_KEYS}
+             "NB_BUILD_QUANTIZED_KEYS": lib.BUILD_QUANTIZED_KEYS,
+             "NB_FAULT_DROP_LOOKBACK": lib.FAULT_DROP_LOOKBACK,
+             "NB_LEARNED_STACK_CAP": lib.LEARNED_STACK_CAP,
+             "NB_POLICY_BOUND_ACCEPT": lib.POLICY_BOUND_ACCEPT, "NB_MLP_PARAMS": lib.MLP_PARAMS}
     for name, value in pairs.items():
         assert h[name] == value, (name, h[name], value)
     assert h["NB_BATCH_CONFIG_COUNT"] == h["NB_PAIR_CONFIG_COUNT"] + h["NB_SYM_CONFIG_COUNT"]
@@ -93,3 +96,38 @@ def test_record_sets_per_traversal():
         assert not build_mask_for(opening, precision) & BUILD_QUANTIZED_KEYS
     for opening, precision in (("theta", "f32c"), ("group", "f32c"), ("learned", "f32c")):
         assert build_mask_for(opening, precision) & BUILD_QUANTIZED_KEYS
+
+
+def test_policy_file_round_trip_and_rejections(tmp_path, cuda_lib):
+    """nb_policy_save / nb_policy_load are host-side: a saved network and its settings load back
+    bit for bit; files with another magic line, network shape, parameter count, a malformed value
+    or unknown flags are rejected with NB_ERR_INVALID_ARG."""
+    import numpy as np
+
+    from nbody.lib import NBodyError, policy_load, policy_save
+    rng = np.random.default_rng(4)
+    params = rng.normal(size=1377).astype(np.float32) * np.float32(3.7)
+    params[5] = np.float32(1e-38)  # subnormal-adjacent and extreme values survive the text form
+    params[6] = np.float32(-3.4e38)
+    path = str(tmp_path / "policy.txt")
+    policy_save(path, params, -4.125, 0.3, 2 ** 31 - 1, 1)
+    got, tau, theta, cap, flags = policy_load(path)
+    np.testing.assert_array_equal(got, params)
+    assert (tau, theta, cap, flags) == (-4.125, 0.3, 2 ** 31 - 1, 1)
+    text = open(path).read().splitlines()
+    assert text[0] == "nbody-gb300 opening policy 1" and text[6] == "params 1377"
+    variants = {
+        "magic": ["nbody opening policy 2"] + text[1:],
+        "shape": text[:1] + ["network 8 64 64 1 relu"] + text[2:],
+        "count": text[:6] + ["params 1376"] + text[7:-1],
+        "value": text[:10] + ["nan-ish"] + text[11:],
+        "flags": text[:5] + ["flags 6"] + text[6:],
+        "short": text[:-1],
+    }
+    for name, lines in variants.items():
+        bad = str(tmp_path / f"bad_{name}.txt")
+        open(bad, "w").write("\n".join(lines) + "\n")
+        with pytest.raises(NBodyError, match="INVALID_ARG"):
+            policy_load(bad)
+    with pytest.raises(ValueError):
+        policy_save(path, params[:10], -4.0, 0.3, 1, 1)
