@@ -13,4 +13,10 @@ public:
     // octree.buildOctree -> nb_bh_build; computeAccelerations -> nb_bh_accel
     void buildOctree();
     void computeAccelerations();
+
+private:
+    nb_graph* stepGraph = nullptr;  // one captured leapfrog step (--graph)
+    float* d_policy = nullptr;      // network of --opening=learned
+    nb_opening openingRule() const;
+    void loadPolicy();
 };

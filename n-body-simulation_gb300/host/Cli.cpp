@@ -11,13 +11,14 @@ const std::vector<std::string>& Cli::known() {
         "num_wi_AABB", "num_wi_com", "max_level_top_octree", "storage_size_param",
         "stack_size_param", "block_size", "algorithm", "energy", "sort_bodies", "use_gpus",
         "wg_size_barnes_hut", "opt_stage",
-        // additions: unit system, softening, arithmetic and opening rule
-        "G", "epsilon2", "precision", "opening", "help"};
+        // additions: unit system, softening, arithmetic, opening rule and its policy file,
+        // graph replay of Barnes-Hut steps
+        "G", "epsilon2", "precision", "opening", "policy", "graph", "help"};
     return k;
 }
 
 static bool is_bool_option(const std::string& k) {
-    return k == "energy" || k == "sort_bodies" || k == "use_gpus" || k == "help";
+    return k == "energy" || k == "sort_bodies" || k == "use_gpus" || k == "graph" || k == "help";
 }
 
 Cli::Cli(int argc, char** argv) {

@@ -10,6 +10,8 @@ bool configuration::use_GPUs = true;
 double configuration::G = 0.0;
 std::string configuration::precision = "f64";
 std::string configuration::opening = "theta";
+std::string configuration::policyFile;
+bool configuration::useGraph = false;
 
 int configuration::naive_algorithm::blockSize = 64;
 int configuration::naive_algorithm::optimization_stage = 2;

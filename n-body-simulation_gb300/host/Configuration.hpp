@@ -19,7 +19,9 @@ extern bool use_GPUs;
 // and FP64 pair arithmetic; these select another unit system and the precision form
 extern double G;             // 0 = the reference's G (nBodyAlgorithm.hpp:55-61)
 extern std::string precision;  // "f64" (default), "f64_ieee", "f32c", "df64"
-extern std::string opening;    // "theta" (default, the reference's rule) or "group"
+extern std::string opening;    // "theta" (default, the reference's rule), "group", "learned"
+extern std::string policyFile; // opening-policy file of --opening=learned (nb_policy_load)
+extern bool useGraph;          // replay unvisualised Barnes-Hut steps from a captured CUDA graph
 
 namespace naive_algorithm {
 extern int blockSize;

@@ -1,9 +1,9 @@
 // NaiveAlgorithm.cpp -- the loop of NaiveAlgorithm::startSimulation (NaiveAlgorithm.cpp:15-260)
 // over the C ABI: initial accelerations, then per step leapfrog part 1, accelerations, leapfrog
-// part 2, with positions/velocities/|a|/energy captured on visualised steps.
+// part 2, with positions/velocities/|a|/energy captured on visualised steps. All work goes to
+// one stream; the host waits only at visualised steps (see nBodyAlgorithm.hpp).
 #include "NaiveAlgorithm.hpp"
 
-#include <chrono>
 #include <cmath>
 #include <iostream>
 
@@ -15,16 +15,11 @@ NaiveAlgorithm::NaiveAlgorithm(double dt, double tEnd, double vs, std::string& o
 void NaiveAlgorithm::computeAccelerations() {
     nb_throw_if(nb_naive_accel(ctx, d_m, d_x, d_y, d_z, d_ax, d_ay, d_az, n, G,
                                configuration::epsilon2, precisionMode(),
-                               configuration::naive_algorithm::blockSize, nullptr),
+                               configuration::naive_algorithm::blockSize, stream),
                 "nb_naive_accel");
-    sync();
 }
 
 void NaiveAlgorithm::startSimulation(const SimulationData& d) {
-    using clk = std::chrono::steady_clock;
-    auto ms = [](clk::time_point a, clk::time_point b) {
-        return std::chrono::duration<double, std::milli>(b - a).count();
-    };
     positions_x[0] = d.positions_x;
     positions_y[0] = d.positions_y;
     positions_z[0] = d.positions_z;
@@ -40,42 +35,41 @@ void NaiveAlgorithm::startSimulation(const SimulationData& d) {
 
     double time = 0.0, sinceVis = 0.0;
     d_type::int_t step = 0;
-    auto a0 = clk::now();
+    int a0 = phases.mark(stream);
     computeAccelerations();
-    timer.addTimeToSequence("Acceleration Kernel Time", ms(a0, clk::now()));
-    if (configuration::compute_energy) computeEnergy(step);
+    phases.span("Acceleration Kernel Time", a0, phases.mark(stream));
     storeAccelerations(step);
+    if (configuration::compute_energy) computeEnergy(step);
+    finishVisualisedStep(step, d);
     std::cout << "Finished initial step " << step << std::endl << std::endl;
     time += dt;
     sinceVis += dt;
     step += 1;
     while (time <= t_end + 0.000001) {
         const bool vis = std::abs(sinceVis - visualizationStepWidth) < 0.000001;
-        auto t0 = clk::now();
+        const int t0 = phases.mark(stream);
         leapfrogPart1();
-        timer.addTimeToSequence("Leapfrog Part 1", ms(t0, clk::now()));
-        if (vis) {
-            download(d_x, positions_x[step]);
-            download(d_y, positions_y[step]);
-            download(d_z, positions_z[step]);
-        }
-        auto t1 = clk::now();
+        const int t1 = phases.mark(stream);
+        if (vis) stagePositions();
+        const int t2 = phases.mark(stream);
         computeAccelerations();
-        timer.addTimeToSequence("Acceleration Kernel Time", ms(t1, clk::now()));
-        auto t2 = clk::now();
+        const int t3 = phases.mark(stream);
         leapfrogPart2();
-        timer.addTimeToSequence("Leapfrog Part 2", ms(t2, clk::now()));
+        const int t4 = phases.mark(stream);
+        phases.span("Leapfrog Part 1", t0, t1);
+        phases.span("Acceleration Kernel Time", t2, t3);
+        phases.span("Leapfrog Part 2", t3, t4);
         if (vis) {
+            stageVelocitiesAndAccelerations(step);
+            finishVisualisedStep(step, d);
             std::cout << "Finished step " << step << std::endl << std::endl;
-            storeAccelerations(step);
-            download(d_vx, velocities_x[step]);
-            download(d_vy, velocities_y[step]);
-            download(d_vz, velocities_z[step]);
-            if (configuration::compute_energy) computeEnergy(step);
             step += 1;
             sinceVis = 0.0;
+        } else {
+            syncIfManyPending();
         }
         time += dt;
         sinceVis += dt;
     }
+    sync();
 }

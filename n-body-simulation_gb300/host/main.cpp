@@ -18,7 +18,8 @@ static void usage() {
                  "  times are <double><h|d|m|y>; options: --theta --block_size --opt_stage"
                  " --energy --sort_bodies --max_level_top_octree --storage_size_param"
                  " --stack_size_param --num_wi_* --wg_size_barnes_hut --use_gpus"
-                 " --G --epsilon2 --precision=<f64|f64_ieee|f32c|df64> --opening=<theta|group>\n";
+                 " --G --epsilon2 --precision=<f64|f64_ieee|f32c|df64>"
+                 " --opening=<theta|group|learned> --policy=<file> --graph\n";
 }
 
 static int run(int argc, char** argv) {
@@ -48,6 +49,10 @@ static int run(int argc, char** argv) {
     if (options.has("epsilon2")) configuration::epsilon2 = options.number("epsilon2");
     if (options.has("precision")) configuration::precision = options.str("precision");
     if (options.has("opening")) configuration::opening = options.str("opening");
+    if (options.has("policy")) configuration::policyFile = options.str("policy");
+    if (options.has("graph")) configuration::useGraph = options.flag("graph");
+    if (configuration::opening == "learned" && configuration::policyFile.empty())
+        throw std::invalid_argument("--opening=learned needs --policy=<file>");
 
     const std::string algorithm = options.str("algorithm");
     if (algorithm == "naive") {

@@ -1,5 +1,6 @@
 // nBodyAlgorithm.cpp -- shared simulation shell (nBodyAlgorithm.cpp:11-411 of the reference:
-// energy, |a| capture, velocity adjustment, ParaView .pvd/.vtp, lastState.csv, times.json).
+// energy, |a| capture, velocity adjustment, ParaView .pvd/.vtp, lastState.csv, times.json), with
+// the stream, event timing, staging and background .vtp writing described in the header.
 #include "nBodyAlgorithm.hpp"
 
 #include <cuda_runtime.h>
@@ -21,6 +22,49 @@ static void cuda_throw_if(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// ---------------------------------------------------------------------------------------------
+// PhaseTimer
+// ---------------------------------------------------------------------------------------------
+PhaseTimer::~PhaseTimer() {
+    for (void* e : pool) cudaEventDestroy((cudaEvent_t)e);
+    for (void* e : marks) cudaEventDestroy((cudaEvent_t)e);
+}
+
+int PhaseTimer::mark(nb_stream_t stream) {
+    cudaEvent_t e = nullptr;
+    if (!pool.empty()) {
+        e = (cudaEvent_t)pool.back();
+        pool.pop_back();
+    } else {
+        cuda_throw_if(cudaEventCreate(&e), "cudaEventCreate");
+    }
+    marks.push_back(e);
+    cuda_throw_if(cudaEventRecord(e, (cudaStream_t)stream), "cudaEventRecord");
+    return (int)marks.size() - 1;
+}
+
+void PhaseTimer::span(const std::string& sequence, int from, int to) {
+    spans.push_back({sequence, {from, to}});
+}
+
+void PhaseTimer::flush(TimeMeasurement& timer) {
+    if (marks.empty()) return;
+    cuda_throw_if(cudaEventSynchronize((cudaEvent_t)marks.back()), "cudaEventSynchronize");
+    for (auto& [name, ft] : spans) {
+        float ms = 0.f;
+        cuda_throw_if(cudaEventElapsedTime(&ms, (cudaEvent_t)marks[ft.first],
+                                           (cudaEvent_t)marks[ft.second]),
+                      "cudaEventElapsedTime");
+        timer.addTimeToSequence(name, ms);
+    }
+    spans.clear();
+    pool.insert(pool.end(), marks.begin(), marks.end());
+    marks.clear();
+}
+
+// ---------------------------------------------------------------------------------------------
+// nBodyAlgorithm
+// ---------------------------------------------------------------------------------------------
 nBodyAlgorithm::nBodyAlgorithm(double dt_, double t_end_, double vs, std::string& outDir)
     : outputDirectory(outDir), dt(dt_), t_end(t_end_), visualizationStepWidth(vs) {
     if (configuration::G != 0) {
@@ -35,14 +79,24 @@ nBodyAlgorithm::nBodyAlgorithm(double dt_, double t_end_, double vs, std::string
         throw std::invalid_argument(
             "use_gpus=false: this build runs the force paths on the GPU only");
     nb_throw_if(nb_ctx_create(0, &ctx), "nb_ctx_create");
+    cudaStream_t s = nullptr;
+    cuda_throw_if(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+    stream = (nb_stream_t)s;
     cudaDeviceProp prop{};
     if (cudaGetDeviceProperties(&prop, 0) == cudaSuccess) deviceName = prop.name;
 }
 
 nBodyAlgorithm::~nBodyAlgorithm() {
+    try {
+        stopWriter();
+    } catch (...) {
+    }
+    if (stream) cudaStreamSynchronize((cudaStream_t)stream);
     for (double* p : {d_m, d_x, d_y, d_z, d_vx, d_vy, d_vz, d_ax, d_ay, d_az, d_vhx, d_vhy, d_vhz,
                       d_energy})
         if (p) cudaFree(p);
+    if (h_stage) cudaFreeHost(h_stage);
+    if (stream) cudaStreamDestroy((cudaStream_t)stream);
     nb_ctx_destroy(ctx);
 }
 
@@ -53,19 +107,19 @@ void nBodyAlgorithm::upload(const SimulationData& d) {
                        &d_ay, &d_az, &d_vhx, &d_vhy, &d_vhz};
     for (double** a : arrs) cuda_throw_if(cudaMalloc(a, bytes), "cudaMalloc");
     cuda_throw_if(cudaMalloc(&d_energy, 4 * sizeof(double)), "cudaMalloc");
+    cuda_throw_if(cudaMallocHost(&h_stage, (9 * (size_t)n + 4) * sizeof(double)),
+                  "cudaMallocHost");
     const std::vector<double>* src[] = {&d.mass, &d.positions_x, &d.positions_y, &d.positions_z,
                                         &d.velocities_x, &d.velocities_y, &d.velocities_z};
     double* dst[] = {d_m, d_x, d_y, d_z, d_vx, d_vy, d_vz};
+    cudaStream_t s = (cudaStream_t)stream;
     for (int k = 0; k < 7; ++k)
-        cuda_throw_if(cudaMemcpy(dst[k], src[k]->data(), bytes, cudaMemcpyHostToDevice), "upload");
+        cuda_throw_if(cudaMemcpyAsync(dst[k], src[k]->data(), bytes, cudaMemcpyHostToDevice, s),
+                      "upload");
     for (double* a : {d_ax, d_ay, d_az, d_vhx, d_vhy, d_vhz})
-        cuda_throw_if(cudaMemset(a, 0, bytes), "cudaMemset");
-}
-
-void nBodyAlgorithm::download(const double* dev, std::vector<double>& host) const {
-    host.resize(n);
-    cuda_throw_if(cudaMemcpy(host.data(), dev, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost),
-                  "download");
+        cuda_throw_if(cudaMemsetAsync(a, 0, bytes, s), "cudaMemset");
+    // the host vectors may change after this call returns
+    cuda_throw_if(cudaStreamSynchronize(s), "upload");
 }
 
 nb_precision nBodyAlgorithm::precisionMode() const {
@@ -76,44 +130,101 @@ nb_precision nBodyAlgorithm::precisionMode() const {
     throw std::invalid_argument("precision must be f64, f64_ieee, f32c or df64");
 }
 
-void nBodyAlgorithm::sync() { nb_throw_if(nb_sync(ctx, nullptr), "nb_sync"); }
+void nBodyAlgorithm::sync() {
+    nb_throw_if(nb_sync(ctx, stream), "nb_sync");
+    phases.flush(timer);
+}
+
+void nBodyAlgorithm::syncIfManyPending() {
+    if (phases.pending() > 1024) sync();
+}
 
 void nBodyAlgorithm::leapfrogPart1() {
     nb_throw_if(nb_leapfrog_kick_drift(ctx, d_vhx, d_vhy, d_vhz, d_vx, d_vy, d_vz, d_x, d_y, d_z,
-                                       d_ax, d_ay, d_az, n, dt, nullptr),
+                                       d_ax, d_ay, d_az, n, dt, stream),
                 "leapfrog part 1");
-    sync();
 }
 
 void nBodyAlgorithm::leapfrogPart2() {
     nb_throw_if(nb_leapfrog_kick(ctx, d_vx, d_vy, d_vz, d_vhx, d_vhy, d_vhz, d_ax, d_ay, d_az, n,
-                                 dt, nullptr),
+                                 dt, stream),
                 "leapfrog part 2");
-    sync();
 }
 
-// nBodyAlgorithm.cpp:11-86
-void nBodyAlgorithm::computeEnergy(d_type::int_t step) {
-    nb_throw_if(nb_energy(ctx, d_m, d_x, d_y, d_z, d_vx, d_vy, d_vz, n, G, d_energy, nullptr),
+static void stage(double* host, const double* dev, size_t count, nb_stream_t s) {
+    cuda_throw_if(cudaMemcpyAsync(host, dev, count * sizeof(double), cudaMemcpyDeviceToHost,
+                                  (cudaStream_t)s),
+                  "staging copy");
+}
+
+// nBodyAlgorithm.cpp:11-86 (the sums run on the GPU; the result is staged for the step)
+void nBodyAlgorithm::computeEnergy(d_type::int_t) {
+    nb_throw_if(nb_energy(ctx, d_m, d_x, d_y, d_z, d_vx, d_vy, d_vz, n, G, d_energy, stream),
                 "nb_energy");
-    sync();
-    double e[4];
-    cuda_throw_if(cudaMemcpy(e, d_energy, sizeof(e), cudaMemcpyDeviceToHost), "energy");
-    kineticEnergy[step] = e[0];
-    potentialEnergy[step] = e[1];
-    totalEnergy[step] = e[2];
-    virialEquilibrium[step] = e[3];
+    stage(h_stage + 9 * (size_t)n, d_energy, 4, stream);
+    energy_staged = true;
 }
 
-// nBodyAlgorithm.cpp:88-102: keeps |a| only
-void nBodyAlgorithm::storeAccelerations(d_type::int_t step) {
-    std::vector<double> ax, ay, az;
-    download(d_ax, ax);
-    download(d_ay, ay);
-    download(d_az, az);
-    auto& out = acceleration[step];
-    out.resize(n);
-    for (d_type::int_t i = 0; i < n; ++i) out[i] = std::sqrt(ax[i] * ax[i] + ay[i] * ay[i] + az[i] * az[i]);
+// nBodyAlgorithm.cpp:88-102 (|a| is formed when the step is finished)
+void nBodyAlgorithm::storeAccelerations(d_type::int_t) {
+    stage(h_stage + 6 * (size_t)n, d_ax, n, stream);
+    stage(h_stage + 7 * (size_t)n, d_ay, n, stream);
+    stage(h_stage + 8 * (size_t)n, d_az, n, stream);
+}
+
+void nBodyAlgorithm::stagePositions() {
+    stage(h_stage + 0 * (size_t)n, d_x, n, stream);
+    stage(h_stage + 1 * (size_t)n, d_y, n, stream);
+    stage(h_stage + 2 * (size_t)n, d_z, n, stream);
+}
+
+void nBodyAlgorithm::stageVelocitiesAndAccelerations(d_type::int_t step) {
+    stage(h_stage + 3 * (size_t)n, d_vx, n, stream);
+    stage(h_stage + 4 * (size_t)n, d_vy, n, stream);
+    stage(h_stage + 5 * (size_t)n, d_vz, n, stream);
+    storeAccelerations(step);
+    if (configuration::compute_energy) computeEnergy(step);
+}
+
+void nBodyAlgorithm::finishVisualisedStep(d_type::int_t step, const SimulationData& d) {
+    sync();
+    const size_t nn = n;
+    const double* h = h_stage;
+    if (step > 0) {  // step 0 keeps the input positions and the adjusted input velocities
+        positions_x[step].assign(h, h + nn);
+        positions_y[step].assign(h + nn, h + 2 * nn);
+        positions_z[step].assign(h + 2 * nn, h + 3 * nn);
+        velocities_x[step].assign(h + 3 * nn, h + 4 * nn);
+        velocities_y[step].assign(h + 4 * nn, h + 5 * nn);
+        velocities_z[step].assign(h + 5 * nn, h + 6 * nn);
+    }
+    auto& acc = acceleration[step];
+    acc.resize(nn);
+    const double *ax = h + 6 * nn, *ay = h + 7 * nn, *az = h + 8 * nn;
+    for (size_t i = 0; i < nn; ++i) acc[i] = std::sqrt(ax[i] * ax[i] + ay[i] * ay[i] + az[i] * az[i]);
+    VtpJob job{step, &positions_x[step], &positions_y[step], &positions_z[step],
+               &velocities_x[step], &velocities_y[step], &velocities_z[step], &acc,
+               {0, 0, 0, 0}};
+    if (energy_staged) {
+        const double* e = h + 9 * nn;
+        kineticEnergy[step] = e[0];
+        potentialEnergy[step] = e[1];
+        totalEnergy[step] = e[2];
+        virialEquilibrium[step] = e[3];
+        for (int k = 0; k < 4; ++k) job.energy[k] = e[k];
+        energy_staged = false;
+    }
+    {
+        std::lock_guard<std::mutex> lock(writer_mutex);
+        if (!writer_error.empty()) throw std::runtime_error("vtp writer: " + writer_error);
+        writer_data = &d;
+        writer_jobs.push_back(job);
+        if (!writer.joinable()) {
+            runDirectory();
+            writer = std::thread(&nBodyAlgorithm::writerLoop, this);
+        }
+    }
+    writer_cv.notify_one();
 }
 
 // nBodyAlgorithm.cpp:104-127: only the step-0 output velocities change
@@ -133,6 +244,55 @@ void nBodyAlgorithm::adjustVelocities(const SimulationData& d) {
     }
 }
 
+// <vs_dir>/<timestamp>/, created when the first visualised step is handed to the writer
+// (nBodyAlgorithm.cpp:129-251 names it by the time of the output)
+std::string nBodyAlgorithm::runDirectory() {
+    if (lastOutputPath.empty()) {
+        std::time_t now = std::time(nullptr);
+        std::string stamp = std::ctime(&now);
+        std::replace(stamp.begin(), stamp.end(), ' ', '_');
+        stamp = stamp.substr(0, stamp.size() - 1);
+        lastOutputPath = outputDirectory + '/' + stamp + '/';
+        std::filesystem::create_directories(lastOutputPath);
+    }
+    return lastOutputPath;
+}
+
+void nBodyAlgorithm::writerLoop() {
+    for (;;) {
+        VtpJob job{};
+        const SimulationData* data = nullptr;
+        std::string base;
+        {
+            std::unique_lock<std::mutex> lock(writer_mutex);
+            writer_cv.wait(lock, [&] { return writer_stop || !writer_jobs.empty(); });
+            if (writer_jobs.empty()) return;  // stop requested and nothing left
+            job = writer_jobs.front();
+            writer_jobs.pop_front();
+            data = writer_data;
+            base = lastOutputPath;
+        }
+        try {
+            writeVtp(job, *data, base + "simulation_step" + std::to_string(job.step) + ".vtp");
+        } catch (const std::exception& e) {
+            std::lock_guard<std::mutex> lock(writer_mutex);
+            writer_error = e.what();
+            return;
+        }
+    }
+}
+
+void nBodyAlgorithm::stopWriter() {
+    {
+        std::lock_guard<std::mutex> lock(writer_mutex);
+        writer_stop = true;
+    }
+    writer_cv.notify_all();
+    if (writer.joinable()) writer.join();
+    writer_stop = false;
+    if (!writer_error.empty()) throw std::runtime_error("vtp writer: " + writer_error);
+}
+
 static int bodyClassCode(const std::string& c) {  // nBodyAlgorithm.cpp:298-342
     static const char* kClasses[] = {"AMO", "APO", "ATE", "IEO", "MCA", "IMB", "MBA", "OMB", "CEN",
                                      "TJN", "TNO", "AST", "PAA", "HYA", "STA", "DWA", "PLA", "SAT"};
@@ -141,9 +301,10 @@ static int bodyClassCode(const std::string& c) {  // nBodyAlgorithm.cpp:298-342
     return 0;
 }
 
-void nBodyAlgorithm::writeVtp(size_t i, const SimulationData& d, const std::string& path) {
+void nBodyAlgorithm::writeVtp(const VtpJob& job, const SimulationData& d, const std::string& path) {
     std::ofstream f(path);
-    const size_t np = positions_x[i].size();
+    if (!f) throw std::runtime_error("cannot write " + path);
+    const size_t np = job.px->size();
     f << "<?xml version=\"1.0\"?>" << '\n'
       << R"(<VTKFile type="PolyData" version="0.1" byte_order="LittleEndian" header_type="UInt64">)"
       << '\n'
@@ -153,19 +314,19 @@ void nBodyAlgorithm::writeVtp(size_t i, const SimulationData& d, const std::stri
       << R"(<DataArray type="Float64" Name="position" NumberOfComponents="3" format="ascii">)"
       << '\n';
     for (size_t j = 0; j < np; ++j)
-        f << positions_x[i][j] << " " << positions_y[i][j] << " " << positions_z[i][j] << '\n';
+        f << (*job.px)[j] << " " << (*job.py)[j] << " " << (*job.pz)[j] << '\n';
     f << "</DataArray>" << '\n' << "</Points>" << '\n' << "<PointData>" << '\n'
       << R"(<DataArray type="Int32" Name="body_id" NumberOfComponents="1" format="ascii">)" << '\n';
     for (size_t j = 0; j < np; ++j) f << j << '\n';
     f << "</DataArray>" << '\n'
       << R"(<DataArray type="Float64" Name="velocity" NumberOfComponents="3" format="ascii">)"
       << '\n';
-    for (size_t j = 0; j < velocities_x[i].size(); ++j)
-        f << velocities_x[i][j] << " " << velocities_y[i][j] << " " << velocities_z[i][j] << '\n';
+    for (size_t j = 0; j < job.vx->size(); ++j)
+        f << (*job.vx)[j] << " " << (*job.vy)[j] << " " << (*job.vz)[j] << '\n';
     f << "</DataArray>" << '\n'
       << R"(<DataArray type="Float64" Name="acceleration" NumberOfComponents="1" format="ascii">)"
       << '\n';
-    for (size_t j = 0; j < np; ++j) f << acceleration[i][j] << '\n';
+    for (size_t j = 0; j < np; ++j) f << (*job.acc)[j] << '\n';
     f << "</DataArray>" << '\n'
       << R"(<DataArray type="Float64" Name="mass" NumberOfComponents="1" format="ascii">)" << '\n';
     for (double m : d.mass) f << m << '\n';
@@ -189,12 +350,10 @@ void nBodyAlgorithm::writeVtp(size_t i, const SimulationData& d, const std::stri
     const bool e = configuration::compute_energy;
     const char* names[] = {"kinetic energy", "potential energy", "total energy",
                            "virial equilibrium"};
-    std::map<d_type::int_t, double>* vals[] = {&kineticEnergy, &potentialEnergy, &totalEnergy,
-                                              &virialEquilibrium};
     for (int k = 0; k < 4; ++k) {
         f << "<DataArray type=\"Float64\" Name=\"" << names[k]
           << "\" NumberOfTuples=\"1\" format=\"ascii\">" << '\n';
-        if (e) f << (*vals[k])[(d_type::int_t)i] << '\n';
+        if (e) f << job.energy[k] << '\n';
         else f << 0 << '\n';
         f << "</DataArray>" << '\n';
     }
@@ -202,15 +361,11 @@ void nBodyAlgorithm::writeVtp(size_t i, const SimulationData& d, const std::stri
 }
 
 // nBodyAlgorithm.cpp:129-251: <vs_dir>/<timestamp>/ with times.json, lastState.csv,
-// simulation.pvd and simulation_step<i>.vtp
+// simulation.pvd and simulation_step<i>.vtp (the .vtp files were written by the background
+// writer while the simulation ran; this waits for it)
 void nBodyAlgorithm::generateParaViewOutput(const SimulationData& d) {
-    std::time_t now = std::time(nullptr);
-    std::string stamp = std::ctime(&now);
-    std::replace(stamp.begin(), stamp.end(), ' ', '_');
-    stamp = stamp.substr(0, stamp.size() - 1);
-    const std::string base = outputDirectory + '/' + stamp + '/';
-    std::filesystem::create_directories(base);
-    lastOutputPath = base;
+    stopWriter();
+    const std::string base = runDirectory();
     timer.exportJSON(base + "times.json");
     outputLastState(base + "lastState.csv");
     std::ofstream pvd(base + "/simulation.pvd");
@@ -222,7 +377,6 @@ void nBodyAlgorithm::generateParaViewOutput(const SimulationData& d) {
         const std::string name = "simulation_step" + std::to_string(i) + ".vtp";
         pvd << "<DataSet timestep=\"" << i << "\" " << R"(group="" part="0" file=")" << name
             << "\"/>" << '\n';
-        writeVtp(i, d, base + name);
     }
     pvd << "</Collection>" << '\n' << "</VTKFile>" << '\n';
 }

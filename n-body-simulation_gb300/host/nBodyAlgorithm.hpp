@@ -2,10 +2,20 @@
 // output. Mirrors src/simulationBackend/nBodyAlgorithm.hpp:19-109 (same members and methods);
 // the SYCL buffers become device arrays owned by the object and the kernels calls into
 // libnbody_cuda.so.
+//
+// Unlike the reference, whose every kernel submission waits for the device (.wait()), the loop
+// here enqueues all work on one CUDA stream and only waits at visualised steps and at the end:
+// phase durations come from CUDA events read back at those points, visualised arrays are copied
+// into pinned staging buffers on the stream, and the .vtp files of visualised steps are written
+// by a background thread while the simulation goes on.
 #pragma once
 
+#include <condition_variable>
+#include <deque>
 #include <map>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "Configuration.hpp"
@@ -15,6 +25,23 @@
 
 // Turns an nb_status into the reference's exception style.
 void nb_throw_if(nb_status st, const char* what);
+
+// Durations of named phases from CUDA events on a stream, resolved in batches: mark() records an
+// event, span() pairs two marks under a timing-sequence name, flush() waits for the last mark and
+// appends every pending span (ms) to a TimeMeasurement, returning the events to a pool.
+class PhaseTimer {
+public:
+    ~PhaseTimer();
+    int mark(nb_stream_t stream);
+    void span(const std::string& sequence, int from, int to);
+    void flush(TimeMeasurement& timer);
+    size_t pending() const { return marks.size(); }
+
+private:
+    std::vector<void*> pool;   // cudaEvent_t
+    std::vector<void*> marks;  // events recorded since the last flush
+    std::vector<std::pair<std::string, std::pair<int, int>>> spans;
+};
 
 class nBodyAlgorithm {
 public:
@@ -42,6 +69,7 @@ public:
 protected:
     // device state (FP64 structure of arrays)
     nb_ctx* ctx = nullptr;
+    nb_stream_t stream = nullptr;  // every launch and copy of the run
     d_type::int_t n = 0;
     double *d_m = nullptr, *d_x = nullptr, *d_y = nullptr, *d_z = nullptr;
     double *d_vx = nullptr, *d_vy = nullptr, *d_vz = nullptr;
@@ -49,14 +77,44 @@ protected:
     double *d_vhx = nullptr, *d_vhy = nullptr, *d_vhz = nullptr;
     double* d_energy = nullptr;
     std::string deviceName;
+    PhaseTimer phases;
 
     void upload(const SimulationData& simulationData);
-    void download(const double* dev, std::vector<double>& host) const;
     nb_precision precisionMode() const;
     void leapfrogPart1();
     void leapfrogPart2();
+    // Waits for the stream, checks the device error word and moves the pending phase times into
+    // `timer`; also done every few hundred marks so that the event pool stays bounded.
     void sync();
+    void syncIfManyPending();
+
+    // Visualised step `step`: positions are staged right after leapfrog part 1 (stagePositions),
+    // velocities, |a| and energies after part 2 (stageVelocitiesAndAccelerations); finishStep
+    // waits for the stream, moves the staged data into the output maps and hands the step to
+    // the .vtp writer.
+    void stagePositions();
+    void stageVelocitiesAndAccelerations(d_type::int_t step);
+    void finishVisualisedStep(d_type::int_t step, const SimulationData& d);
 
 private:
-    void writeVtp(size_t step, const SimulationData& data, const std::string& path);
+    double* h_stage = nullptr;  // pinned: x, y, z, vx, vy, vz, ax, ay, az (n each), energy (4)
+    bool energy_staged = false;
+
+    // background .vtp writer
+    struct VtpJob {
+        size_t step;
+        const std::vector<double>*px, *py, *pz, *vx, *vy, *vz, *acc;
+        double energy[4];
+    };
+    std::thread writer;
+    std::mutex writer_mutex;
+    std::condition_variable writer_cv;
+    std::deque<VtpJob> writer_jobs;
+    bool writer_stop = false;
+    std::string writer_error;
+    const SimulationData* writer_data = nullptr;
+    std::string runDirectory();
+    void writerLoop();
+    void stopWriter();
+    void writeVtp(const VtpJob& job, const SimulationData& data, const std::string& path);
 };

@@ -246,3 +246,46 @@ def time_steps(ctx: Context, t: dict, G: float, steps: int, opening: str, precis
     ctx.sync()
     tree.close()
     return e0.elapsed_time(e1) / steps
+
+
+def error_over_steps(ctx: Context, t: dict, G: float, steps: int, checkpoints, targets,
+                     opening: str, precision: str, theta: float = 0.5, policy=None,
+                     dt: float = 1.0 / 24, eps2: float = EPS2):
+    """Leapfrog run of a state copy (kick + drift, octree build, traversal, kick per step) with
+    the force error of the step's traversal measured at the given step numbers (0 = the initial
+    evaluation): median and p99 relative error of the sampled targets against FP64 naive sums at
+    that step's positions. Returns [{step, median, p99}]."""
+    import torch
+    n = t["m"].numel()
+    pos = [t[k].clone() for k in ("x", "y", "z")]
+    vel = [t[k].clone() for k in ("vx", "vy", "vz")]
+    acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    vh = [torch.zeros_like(a) for a in acc]
+    tree = BHTree(ctx, n, theta=theta)
+    tree.set_records(build_mask_for(opening, precision))
+    tree.build(t["m"], *pos, G)
+    tree.accel(*pos, *acc, G, eps2, "group", "f32c")  # a first |a| for the learned policy
+    if policy is not None:
+        tree.set_policy(*policy)
+    tree.accel(*pos, *acc, G, eps2, opening, precision)
+    out = []
+    cur = {"m": t["m"], "x": pos[0], "y": pos[1], "z": pos[2]}
+
+    def measure(step):
+        ref = fp64_reference(ctx, cur, G, targets)
+        med, p99 = errors(acc, ref, targets)
+        out.append({"step": step, "median": med, "p99": p99})
+
+    marks = set(checkpoints)
+    if 0 in marks:
+        measure(0)
+    for k in range(1, steps + 1):
+        ctx.kick_drift(vh, vel, pos, acc, dt)
+        tree.build(t["m"], *pos, G)
+        tree.accel(*pos, *acc, G, eps2, opening, precision)
+        ctx.kick(vel, vh, acc, dt)
+        if k in marks:
+            measure(k)
+    ctx.sync()
+    tree.close()
+    return out
