@@ -14,8 +14,10 @@
 //     leftmost split of each cell ("first split") stands for the cell.
 //  6. DFS numbering: each sorted position p starts popc(mask[p]) internal cells plus its leaf;
 //     an exclusive scan gives every node its DFS pre-order index and skip link.
-//  7. bottom-up centre of mass: the last child to finish a cell sums the cell's children in
-//     octant order 0..7 (bit-identical to BarnesHutOctree.cpp:304-311).
+//  7. bottom-up centre of mass: leaves one thread each, cells by blocks over chunks of sorted
+//     positions (deepest level first), cells reaching past their chunk by the last child to
+//     arrive; children summed in octant order 0..7 (bit-identical to
+//     BarnesHutOctree.cpp:304-311), node records written with the sums.
 #include <cuda/atomic>
 
 #include <algorithm>
@@ -399,6 +401,7 @@ __global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
 
 struct ComArgs {
     uint32_t n;
+    uint32_t* err;  // device error word
     uint32_t records;  // NB_REC_* sets to compute
     const double *m, *x, *y, *z;
     const double* box;
@@ -408,7 +411,7 @@ struct ComArgs {
     const unsigned long long* mask;
     const uint32_t* base;
     const uint8_t* node_level;
-    const uint32_t *node_first, *node_skip, *node_parent, *node_body, *node_nchild;
+    const uint32_t *node_first, *node_last, *node_skip, *node_parent, *node_body, *node_nchild;
     uint32_t *node_arrive, *node_count;
     double *comx, *comy, *comz, *mass, *q;
     NodeRec64* rec64;
@@ -422,10 +425,38 @@ struct ComArgs {
     float4* sorted4lo;
 };
 
+// Edge of a cell of the given level: box edge * 2^-level by exponent arithmetic (exact, and no
+// FP64 instructions) while the result stays a normal number, else ldexp.
+__device__ __forceinline__ double cell_edge64(double box_edge, int level) {
+    const long long bits = __double_as_longlong(box_edge);
+    const int biased = (int)((bits >> 52) & 0x7ff);
+    if (biased > level + 1 && biased < 0x7ff)
+        return __longlong_as_double(bits - ((long long)level << 52));
+    return ldexp(box_edge, -level);
+}
+
+// RN(c / m) for the rounded product c = RN(x * m) of a leaf (its centre-of-mass numerator over its
+// mass): that quotient is x itself whenever |c / m - x| < ulp(x) / 2, and the difference is known
+// exactly, since the rounding error x * m - c of a product is exact in one FMA. So
+// |x * m - c| * 2^(53 - e(x)) < m (a power-of-two scaling, exact) decides it without a division;
+// the IEEE division remains for the rest (x a power of two, zero, subnormal or extreme, or the
+// quotient rounding to a neighbour of x).
+__device__ __forceinline__ double leaf_quotient(double x, double m, double c) {
+    const long long xb = __double_as_longlong(x);
+    const int biased = (int)((xb >> 52) & 0x7ff);
+    const int s = 1023 + 53 - (biased - 1023);  // biased exponent of 2^(53 - e(x))
+    const bool pow2 = (xb & 0xfffffffffffffll) == 0;
+    if (biased == 0 || biased == 0x7ff || pow2 || s < 1 || s > 2046 || !(m > 0.0))
+        return __ddiv_rn(c, m);
+    const double err = fma(x, m, -c);
+    if (fabs(err) * __longlong_as_double((long long)s << 52) < m) return x;
+    return __ddiv_rn(c, m);
+}
+
 __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double cy, double cz,
                               double sm, double qsum, uint32_t count, int level, uint32_t skip,
                               uint32_t body) {
-    const double edge = ldexp(A.box[6], -level);
+    const double edge = cell_edge64(A.box[6], level);
     const double ox = A.box[7], oy = A.box[8], oz = A.box[9];  // box centre
     // centre = sums / mass: the IEEE quotients when the FP64 records are built (the reference's
     // values, also behind the FP32 pre-test's proven margin), else from one reciprocal (the FP32
@@ -491,93 +522,247 @@ __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double 
         // the spread is a feature of the learned policy, not a sum of the reference: 1/M from the
         // reciprocal, the root in FP32
         NodeAux x;
+        x.spread_rel = 0.f;
+        x.lg_gm = __log2f(fmaxf(q.gm, 1e-37f));
         if (sm != 0) {
             const double s2 = qsum * inv - (gx * gx + gy * gy + gz * gz);
-            x.spread = sqrtf((float)(s2 > 0 ? s2 : 0.0));
-        } else {
-            x.spread = 0.f;
+            const float e = (float)edge;
+            if (e > 0.f) x.spread_rel = sqrtf((float)(s2 > 0 ? s2 : 0.0)) / e;
         }
         x.count = count;
         x.first = A.node_first_pos[idx];
-        x.edge = (float)edge;
         A.aux[idx] = x;
     }
 }
 
-__global__ void com_kernel(ComArgs A) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= A.n) return;
-    const uint32_t idx = A.base[p] + __popcll(A.mask[p]);
-    const uint32_t b = A.ids[p];
+// Sums of internal node `idx` from its children (the reference's octant order 0..7, FP64 adds:
+// bit-identical to BarnesHutOctree.cpp:304-311), its records, and its child list rewritten as the
+// compacted visit-order list the learned traversal reads (emit_kernel wrote it by visit rank).
+__device__ void sum_children(const ComArgs& A, uint32_t idx, bool records) {
+    uint4* cl = reinterpret_cast<uint4*>(A.children + (size_t)idx * 8);
+    const uint4 c0 = __ldcg(cl), c1 = __ldcg(cl + 1);
+    const uint32_t vs[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+    uint32_t list[8];
+    int nch = 0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        list[t] = NB_NONE;
+        if (vs[t] != NB_NONE) list[nch++] = vs[t];
+    }
+    cl[0] = make_uint4(list[0], list[1], list[2], list[3]);
+    cl[1] = make_uint4(list[4], list[5], list[6], list[7]);
+    const bool learned = (A.records & NB_REC_LEARNED) != 0;
+    double sx = 0, sy = 0, sz = 0, sm = 0, sq = 0;
+    uint32_t count = 0;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+        const uint32_t ch = vs[nb_visit_of_octant(o)];
+        if (ch == NB_NONE) continue;
+        sx = __dadd_rn(sx, __ldcg(&A.comx[ch]));
+        sy = __dadd_rn(sy, __ldcg(&A.comy[ch]));
+        sz = __dadd_rn(sz, __ldcg(&A.comz[ch]));
+        sm = __dadd_rn(sm, __ldcg(&A.mass[ch]));
+        if (learned) sq += __ldcg(&A.q[ch]);
+        count += __ldcg(&A.node_count[ch]);
+    }
+    A.comx[idx] = sx;
+    A.comy[idx] = sy;
+    A.comz[idx] = sz;
+    A.mass[idx] = sm;
+    if (learned) A.q[idx] = sq;
+    A.node_count[idx] = count;
+    if (records)
+        write_records(A, idx, sx, sy, sz, sm, sq, count, A.node_level[idx], A.node_skip[idx],
+                      NB_NONE);
+}
+
+// Records of internal node `idx` from its final sums (written earlier by sum_children).
+__device__ void cell_records(const ComArgs& A, uint32_t idx) {
+    const bool learned = (A.records & NB_REC_LEARNED) != 0;
+    write_records(A, idx, __ldcg(&A.comx[idx]), __ldcg(&A.comy[idx]), __ldcg(&A.comz[idx]),
+                  __ldcg(&A.mass[idx]), learned ? __ldcg(&A.q[idx]) : 0.0,
+                  __ldcg(&A.node_count[idx]), A.node_level[idx], A.node_skip[idx], NB_NONE);
+}
+
+// Sums and records of the leaf `idx` (body b at sorted position p). A leaf's centre of mass is
+// its body: the FP64 records keep the reference's quotient (c / m, mostly decided without a
+// division by leaf_quotient), the FP32 records take the body position itself (within their own
+// rounding of that quotient), and the spread of a single body is 0.
+__device__ void leaf_sums(const ComArgs& A, uint32_t idx, uint32_t p, uint32_t b) {
     const double mb = A.m[b];
     const double bx = A.x[b], by = A.y[b], bz = A.z[b];
     const double cx = __dmul_rn(bx, mb), cy = __dmul_rn(by, mb), cz = __dmul_rn(bz, mb);
-    const bool learned = (A.records & NB_REC_LEARNED) != 0;
     A.comx[idx] = cx;
     A.comy[idx] = cy;
     A.comz[idx] = cz;
     A.mass[idx] = mb;
     A.node_count[idx] = 1;
-    if (learned) {  // spread sums and the FP32 body copies of the learned policy
-        const double rx = bx - A.box[7], ry = by - A.box[8], rz = bz - A.box[9];
+    const int level = A.node_level[idx];
+    const uint32_t skip = A.node_skip[idx];
+    const double edge = cell_edge64(A.box[6], level);
+    const double ox = A.box[7], oy = A.box[8], oz = A.box[9];
+    const bool fp64 = (A.records & NB_REC_FP64) != 0;
+    double rcx = bx, rcy = by, rcz = bz;
+    if (fp64 && mb != 0) {
+        rcx = leaf_quotient(bx, mb, cx);
+        rcy = leaf_quotient(by, mb, cy);
+        rcz = leaf_quotient(bz, mb, cz);
+    }
+    if (fp64) {
+        NodeRec64 r;
+        r.cx = mb != 0 ? rcx : 0.0;
+        r.cy = mb != 0 ? rcy : 0.0;
+        r.cz = mb != 0 ? rcz : 0.0;
+        r.mass = mb;
+        r.edge = edge;
+        r.skip = skip;
+        r.body = b;
+        A.rec64[idx] = r;
+    }
+    const double gx = rcx - ox, gy = rcy - oy, gz = rcz - oz;
+    NodeRec32 q;
+    q.cx = mb != 0 ? (float)gx : 1e30f;  // a massless body: far away, contributes exactly 0
+    q.cy = mb != 0 ? (float)gy : 1e30f;
+    q.cz = mb != 0 ? (float)gz : 1e30f;
+    q.gm = (float)(A.G * mb);
+    q.edge2 = (float)(edge * edge);
+    q.skip = skip;
+    q.body = b;
+    q.level = (uint32_t)level;
+    A.rec32[idx] = q;
+    if (A.records & NB_REC_DF) {
+        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), lo2 = lo;
+        if (mb != 0) {
+            float hx, hy, hz;
+            tf_split_diff(rcx, ox, hx, lo.x, lo2.x);
+            tf_split_diff(rcy, oy, hy, lo.y, lo2.y);
+            tf_split_diff(rcz, oz, hz, lo.z, lo2.z);
+            lo.w = (float)(A.G * mb - (double)q.gm);
+        }
+        A.rec32lo[idx] = lo;
+        A.rec32lo2[idx] = lo2;
+    }
+    if (A.records & NB_REC_LEARNED) {  // spread sums and the FP32 body copies of the policy
+        const double rx = bx - ox, ry = by - oy, rz = bz - oz;
         A.q[idx] = mb * (rx * rx + ry * ry + rz * rz);
         const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
-        A.sorted4[p] = make_float4(hx, hy, hz, (float)(A.G * mb));
+        A.sorted4[p] = make_float4(hx, hy, hz, q.gm);
         A.sorted4lo[p] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy),
                                      (float)(rz - (double)hz), 0.f);
+        NodeAux x;
+        x.spread_rel = 0.f;
+        x.count = 1;
+        x.first = p;
+        x.lg_gm = __log2f(fmaxf(q.gm, 1e-37f));
+        A.aux[idx] = x;
     }
+}
+
+// A node whose sums are final arrives at its parent; the last child to arrive sums the parent
+// and climbs on. The acquire-release arrival publishes this thread's sums and, for the last
+// child, makes the siblings' sums visible. Parents have smaller DFS indices, so the climb ends;
+// it is also capped at the tree's depth.
+__device__ void arrive_and_climb(const ComArgs& A, uint32_t idx) {
     uint32_t cur = A.node_parent[idx];
-    while (cur != NB_NONE) {
-        // acquire-release arrival: publishes this child's sums and, for the last child, makes
-        // the siblings' sums visible (one device-scope RMW instead of two full fences)
+    for (int guard = 0; cur != NB_NONE; ++guard) {
+        if (guard > 2 * NB_KEY_LEVELS + 2) {
+            atomicOr(A.err, NB_DEVERR_DEPTH);
+            return;
+        }
         cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrive(A.node_arrive[cur]);
         if (arrive.fetch_add(1u, cuda::memory_order_acq_rel) != A.node_nchild[cur] - 1u) return;
-        // children by visit rank (written by emit_kernel); rewritten below as the compacted
-        // visit-order list the learned traversal reads
-        uint4* cl = reinterpret_cast<uint4*>(A.children + (size_t)cur * 8);
-        const uint4 c0 = __ldcg(cl), c1 = __ldcg(cl + 1);
-        const uint32_t vs[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-        uint32_t list[8];
-        int nch = 0;
-#pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            list[t] = NB_NONE;
-            if (vs[t] != NB_NONE) list[nch++] = vs[t];
-        }
-        cl[0] = make_uint4(list[0], list[1], list[2], list[3]);
-        cl[1] = make_uint4(list[4], list[5], list[6], list[7]);
-        double sx = 0, sy = 0, sz = 0, sm = 0, sq = 0;
-        uint32_t count = 0;
-#pragma unroll
-        for (int o = 0; o < 8; ++o) {  // the reference's octant order 0..7
-            const uint32_t ch = vs[nb_visit_of_octant(o)];
-            if (ch == NB_NONE) continue;
-            sx = __dadd_rn(sx, __ldcg(&A.comx[ch]));
-            sy = __dadd_rn(sy, __ldcg(&A.comy[ch]));
-            sz = __dadd_rn(sz, __ldcg(&A.comz[ch]));
-            sm = __dadd_rn(sm, __ldcg(&A.mass[ch]));
-            if (learned) sq += __ldcg(&A.q[ch]);
-            count += __ldcg(&A.node_count[ch]);
-        }
-        A.comx[cur] = sx;
-        A.comy[cur] = sy;
-        A.comz[cur] = sz;
-        A.mass[cur] = sm;
-        if (learned) A.q[cur] = sq;
-        A.node_count[cur] = count;
+        sum_children(A, cur, true);
         cur = A.node_parent[cur];
     }
 }
 
-// Traversal records of every node from its sums, one thread per node: the FP64 work (divisions,
-// splits, the spread's square root) runs with full warps here instead of on the few threads
-// that climb the tree in com_kernel.
-__global__ void records_kernel(ComArgs A, const uint32_t* __restrict__ info) {
-    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= info[0]) return;
-    write_records(A, idx, A.comx[idx], A.comy[idx], A.comz[idx], A.mass[idx],
-                  (A.records & NB_REC_LEARNED) ? A.q[idx] : 0.0, A.node_count[idx],
-                  A.node_level[idx], A.node_skip[idx], A.node_body[idx]);
+// Centre of mass and records, bottom-up, in chunks of CW consecutive sorted positions. The nodes
+// starting in a chunk are the DFS indices [base[P], base[P + CW]); the ones that also end in it
+// ("local": all leaves and most cells) are summed without atomics, the few cells that reach past
+// their chunk ("global": the ancestors of chunk boundaries) by the arrival climb, which the local
+// nodes whose parent is global start.
+//  * com_leaf_kernel: one thread per sorted position sums its leaf and writes its records (and
+//    the leaf arrives at a global parent);
+//  * com_cells_kernel: one block per chunk sums the chunk's local cells level by level, deepest
+//    first (their children are leaves or deeper local cells), then writes their records in one
+//    sweep over the compacted cell list. FP64 work runs with full warps there: on this part an
+//    FP64 warp instruction costs the FP64 pipe the same time however few of its lanes are active,
+//    so the records stay out of the per-level rounds, where few lanes have a cell.
+constexpr int CW = 2048;                          // sorted positions per chunk
+constexpr int CM_LEVELS = 2 * NB_KEY_LEVELS + 1;  // node levels 0..42
+constexpr int CC_THREADS = 256;                   // threads per block of com_cells_kernel
+constexpr int CC_ROOTS = 512;                     // deferred arrivals kept per chunk
+
+__global__ void __launch_bounds__(256, 5) com_leaf_kernel(ComArgs A) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= A.n) return;
+    const uint32_t idx = A.base[p] + __popcll(A.mask[p]);
+    leaf_sums(A, idx, p, A.ids[p]);
+    const uint32_t par = A.node_parent[idx];
+    if (par == NB_NONE) return;
+    const uint32_t c0 = p / CW * CW, c1 = min(c0 + (uint32_t)CW, A.n);
+    if (A.node_first[par] >= c0 && A.node_last[par] < c1) return;  // summed by its chunk's block
+    arrive_and_climb(A, idx);
+}
+
+__global__ void __launch_bounds__(CC_THREADS) com_cells_kernel(ComArgs A) {
+    __shared__ uint32_t nodes[CW];  // the chunk's local cells, grouped by level
+    __shared__ uint32_t cnt[CM_LEVELS], off[CM_LEVELS], fill[CM_LEVELS];
+    __shared__ uint2 roots[CC_ROOTS];  // (node, thread that summed it)
+    __shared__ uint32_t n_roots;
+    const uint32_t P = blockIdx.x * CW;
+    if (P >= A.n) return;
+    const uint32_t Pend = min(P + (uint32_t)CW, A.n);
+    const uint32_t d0 = A.base[P], d1 = A.base[Pend];
+    for (int l = threadIdx.x; l < CM_LEVELS; l += CC_THREADS) cnt[l] = fill[l] = 0;
+    if (threadIdx.x == 0) n_roots = 0;
+    __syncthreads();
+    for (uint32_t idx = d0 + threadIdx.x; idx < d1; idx += CC_THREADS)
+        if (A.node_body[idx] == NB_NONE && A.node_last[idx] < Pend)
+            atomicAdd(&cnt[min((int)A.node_level[idx], CM_LEVELS - 1)], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int l = 0; l < CM_LEVELS; ++l) {
+            off[l] = run;
+            run += cnt[l];
+        }
+    }
+    __syncthreads();
+    for (uint32_t idx = d0 + threadIdx.x; idx < d1; idx += CC_THREADS) {
+        if (A.node_body[idx] == NB_NONE && A.node_last[idx] < Pend) {
+            const int l = min((int)A.node_level[idx], CM_LEVELS - 1);
+            const uint32_t slot = off[l] + atomicAdd(&fill[l], 1u);
+            if (slot < (uint32_t)CW) nodes[slot] = idx;
+            else atomicOr(A.err, NB_DEVERR_DEPTH);  // a consistent tree never gets here
+        }
+    }
+    __syncthreads();
+    uint32_t total = 0;
+    for (int l = CM_LEVELS - 1; l >= 0; --l) {
+        const uint32_t c = cnt[l];
+        if (c == 0) continue;  // uniform across the block
+        total += c;
+        for (uint32_t k = threadIdx.x; k < c && off[l] + k < (uint32_t)CW; k += CC_THREADS) {
+            const uint32_t idx = nodes[off[l] + k];
+            sum_children(A, idx, false);
+            const uint32_t par = A.node_parent[idx];
+            if (par != NB_NONE && !(par >= d0 && A.node_last[par] < Pend)) {
+                // the parent reaches past the chunk: arrive after the level loop (this thread
+                // wrote the sums, so its release covers them)
+                const uint32_t slot = atomicAdd(&n_roots, 1u);
+                if (slot < (uint32_t)CC_ROOTS) roots[slot] = make_uint2(idx, threadIdx.x);
+                else arrive_and_climb(A, idx);  // no room: arrive now
+            }
+        }
+        __syncthreads();
+    }
+    // records of the local cells, all lanes busy
+    for (uint32_t k = threadIdx.x; k < min(total, (uint32_t)CW); k += CC_THREADS)
+        cell_records(A, nodes[k]);
+    const uint32_t nr = min(n_roots, (uint32_t)CC_ROOTS);
+    for (uint32_t k = 0; k < nr; ++k)
+        if (roots[k].y == threadIdx.x) arrive_and_climb(A, roots[k].x);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -666,6 +851,7 @@ nb_status nb_bh_tree_create(nb_ctx* ctx, uint32_t n_max, const nb_bh_params* par
     } else {
         nb_bh_params_default(&t->params);
     }
+    NB_TRY(nb::radix_prepare());  // before any capture of a build
     Carver sizing;
     carve(t, sizing);
     void* mem = nullptr;
@@ -801,7 +987,9 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     A.base = t->base;
     A.node_level = t->node_level;
     A.node_first = t->node_first;
+    A.node_last = t->node_last;
     A.node_skip = t->node_skip;
+    A.err = ctx->dev_error;
     A.node_parent = t->node_parent;
     A.node_body = t->node_body;
     A.node_nchild = t->node_nchild;
@@ -821,10 +1009,10 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     A.children = t->children;
     A.sorted4 = t->sorted4;
     A.sorted4lo = t->sorted4lo;
-    com_kernel<<<grid, BH_THREADS, 0, s>>>(A);
-    NB_TRY(nb::check_launch("com_kernel"));
-    records_kernel<<<nb::ceil_div(t->node_cap, BH_THREADS), BH_THREADS, 0, s>>>(A, t->info);
-    NB_TRY(nb::check_launch("records_kernel"));
+    com_leaf_kernel<<<grid, BH_THREADS, 0, s>>>(A);
+    NB_TRY(nb::check_launch("com_leaf_kernel"));
+    com_cells_kernel<<<nb::ceil_div(n, CW), CC_THREADS, 0, s>>>(A);
+    NB_TRY(nb::check_launch("com_cells_kernel"));
     NB_TRY(mark(5));
     t->built = true;
     t->built_records = t->records;

@@ -30,10 +30,11 @@ struct __align__(16) NodeRec32 {
 
 // Extra per-node data of the learned opening policy.
 struct __align__(16) NodeAux {
-    float spread;    // mass-weighted rms distance of the cell's bodies from its centre of mass
-    uint32_t count;  // bodies in the cell
-    uint32_t first;  // first sorted position of the cell's bodies (they are contiguous)
-    float edge;
+    float spread_rel;  // mass-weighted rms distance of the cell's bodies from its centre of
+                       // mass, over the cell's edge
+    uint32_t count;    // bodies in the cell
+    uint32_t first;    // first sorted position of the cell's bodies (they are contiguous)
+    float lg_gm;       // log2(max(G * mass, 1e-37))
 };
 
 struct nb_bh_tree {

@@ -59,53 +59,82 @@ __device__ GroupGeo group_geo(bool valid, float px, float py, float pz, float a_
     return g;
 }
 
-// The 8 features of a (group, cell) pair and the cell's class: 0 = decide with the network,
-// 1 = body leaf (accept), 2 = may overlap the group (open), 3 = outside the training range
-// (theta rule), 4 = provably accurate enough (accept). gap = the smallest distance from a member
-// of the group to the cell's centre of mass; d = distance from the group's box centre. Ratios use
-// the fast reciprocal and logarithms the fast base-2 logarithm (features only steer the policy;
-// labels and training use the same function).
-//
-// Class 4 (accept without the network; only when bound_tau > 0): the cell's bodies lie within
-// b = sqrt(3) * edge of its centre of mass, so for a body at distance R >= gap the monopole's
-// force error is at most G M / R^2 * sum_{l>=2} (l+1) (b/R)^l = G M / R^2 * (1/(1-rho)^2 - 1 -
-// 2 rho), rho = b / gap (the multipole series of the potential with a vanishing dipole). When
-// that bound relative to the group's smallest |a| is below bound_tau the cell is accepted.
-__device__ __forceinline__ int cell_features(const NodeRec32& r, const NodeAux& x,
-                                             const GroupGeo& g, float gap, uint32_t count_cap,
-                                             float* f, float bound_tau = 0.f) {
+// FP32 box edge and its base-2 logarithm, for the cell edges: a cell of level L has edge
+// box_edge * 2^-L, exact in FP32 (the edges the records held), formed by exponent arithmetic
+// while the result stays a normal number.
+struct BoxScale {
+    float e0, lg_e0;
+    bool bits;
+    BoxScale() = default;
+    __device__ explicit BoxScale(double box_edge) {
+        e0 = (float)box_edge;
+        lg_e0 = e0 > 0.f ? __log2f(e0) : -128.f;
+        bits = e0 >= 1e-20f;
+    }
+    __device__ __forceinline__ float edge(uint32_t level) const {
+        return bits ? __int_as_float(__float_as_int(e0) - ((int)level << 23))
+                    : ldexpf(e0, -(int)level);
+    }
+};
+
+// The class of a (group, cell) pair: 1 = body leaf (accept), 2 = may overlap the group (gap <=
+// sqrt(3) * edge: open), 3 = outside the training range (theta rule), 0 = for the policy. m2 =
+// squared gap, the smallest squared distance from a member of the group to the cell's centre of
+// mass.
+__device__ __forceinline__ int cell_class(const NodeRec32& r, const NodeAux& x, float m2,
+                                          uint32_t count_cap) {
     if (r.body != NB_NONE) return 1;
-    const float e = x.edge;
-    if (gap <= SQRT3 * e) return 2;
+    if (m2 <= 3.f * r.edge2) return 2;
+    return x.count > count_cap ? 3 : 0;
+}
+
+// The 8 features of a (group, cell) pair and its class (cell_class, plus 4 = provably accurate
+// enough: accept). d = distance from the group's box centre to the cell's centre of mass. The
+// per-cell terms (spread / edge, log2 of G * mass) come from the build; logarithms are the fast
+// base-2 logarithm (features only steer the policy; labels and training use the same function).
+//
+// Class 4 (only when bound_tau > 0): the cell's bodies lie within b = sqrt(3) * edge of its
+// centre of mass, so for a body at distance R >= gap the monopole's force error is at most
+// G M / R^2 * sum_{l>=2} (l+1) (b/R)^l = G M / R^2 * rho^2 (3 - 2 rho) / (1 - rho)^2, rho = b / gap
+// (the multipole series of the potential with a vanishing dipole). When that bound relative to
+// the group's smallest |a| is below bound_tau the cell is accepted; the test is multiplied out,
+// G M b^2 (3 gap - 2 b) < bound_tau a_ref gap^3 (gap - b)^2, so it needs no division.
+__device__ __forceinline__ int cell_features(const NodeRec32& r, const NodeAux& x,
+                                             const GroupGeo& g, const BoxScale& bs, float m2,
+                                             uint32_t count_cap, float* f, float bound_tau = 0.f) {
+    if (r.body != NB_NONE) return 1;
+    if (m2 <= 3.f * r.edge2) return 2;
+    const float e = bs.edge(r.level);
+    const float inv_gap = rsqrtf(m2), gap = m2 * inv_gap;
     if (bound_tau > 0.f) {
-        const float rho = __fdividef(SQRT3 * e, gap), q = 1.f - rho;
-        const float tail = __fdividef(1.f, q * q) - 1.f - 2.f * rho;
-        if (__fdividef(r.gm, gap * gap * g.a_ref) * tail < bound_tau) return 4;
+        const float b = SQRT3 * e, gb = gap - b;
+        if (r.gm * (b * b) * fmaf(3.f, gap, -2.f * b) <
+            bound_tau * g.a_ref * (gap * gap) * gap * (gb * gb))
+            return 4;
     }
     if (x.count > count_cap) return 3;
     const float dx = r.cx - g.cx, dy = r.cy - g.cy, dz = r.cz - g.cz;
     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float inv_d = rsqrtf(d2);
-    const float lg_e = __log2f(e), lg_gap = __log2f(gap);
-    const float lg_d = 0.5f * __log2f(d2);
-    f[0] = (lg_d - lg_e) * 0.25f;
-    f[1] = __fdividef(x.spread, e);
+    const float lg_e = bs.lg_e0 - (float)r.level;
+    const float lg_m2 = __log2f(m2);
+    f[0] = (0.5f * __log2f(d2) - lg_e) * 0.25f;
+    f[1] = x.spread_rel;
     f[2] = __log2f((float)x.count) * 0.0625f;
     f[3] = (float)r.level * 0.0625f;
-    f[4] = g.r * inv_d;
+    f[4] = g.r * rsqrtf(d2);
     // log10(G m / (gap^2 a_ref)) / 4
-    f[5] = (__log2f(fmaxf(r.gm, 1e-37f)) - 2.f * lg_gap - g.lg_aref) * (0.30103f * 0.25f);
-    f[6] = (lg_gap - lg_e) * 0.25f;
-    f[7] = __fdividef(x.spread, gap);
+    f[5] = (x.lg_gm - lg_m2 - g.lg_aref) * (0.30103f * 0.25f);
+    f[6] = (0.5f * lg_m2 - lg_e) * 0.25f;
+    f[7] = x.spread_rel * e * inv_gap;
     return 0;
 }
 
-// Smallest distance from a valid lane's body to (cx, cy, cz), over the whole warp.
-__device__ __forceinline__ float warp_min_dist(bool valid, float px, float py, float pz, float cx,
-                                               float cy, float cz) {
+// Smallest squared distance from a valid lane's body to (cx, cy, cz), over the whole warp.
+__device__ __forceinline__ float warp_min_dist2(bool valid, float px, float py, float pz,
+                                                float cx, float cy, float cz) {
     const float dx = cx - px, dy = cy - py, dz = cz - pz;
     const float inf = __int_as_float(0x7f800000);
-    return sqrtf(warp_min(valid ? fmaf(dx, dx, fmaf(dy, dy, dz * dz)) : inf));
+    return warp_min(valid ? fmaf(dx, dx, fmaf(dy, dy, dz * dz)) : inf);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -114,6 +143,13 @@ __device__ __forceinline__ float warp_min_dist(bool valid, float px, float py, f
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// max(lo, 0), max(hi, 0) as a BF16 pair in one instruction (the ReLU commutes with the rounding).
+__device__ __forceinline__ uint32_t pack_bf16_relu(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
 }
 
 __device__ __forceinline__ void mma16816(float* c, uint32_t a0, uint32_t a1, uint32_t a2,
@@ -130,14 +166,45 @@ __device__ __forceinline__ void mma16816(float* c, uint32_t a0, uint32_t a1, uin
 //  w[4 + (ks*4 + nt)*2 + j]   layer 2, k-step ks, n-tile nt, register j
 //  w[20 + ks*2 + j]           layer 3 (output column 0 only: lanes with g == 0)
 //  b[nt*2 + j], b[8 + nt*2 + j], b[16]: biases of layers 1, 2 and 3 for the lane's columns.
-// They live in shared memory, [index][lane] (conflict-free), shared by the block's warps.
+// They live in shared memory, shared by the block's warps, [lane][index] with row strides of 28
+// and 20 words, so that a layer's fragments come in 16-byte loads (6 for the weights, 5 for the
+// biases) and the 8 lanes of each load phase hit disjoint banks.
 constexpr int MF_W = 24, MF_B = 17;
+constexpr int MF_WS = 28, MF_BS = 20;  // per-lane strides (words)
 struct MlpFragsSmem {
-    const uint32_t* ws;
-    const float* bs;
-    int lane;
-    __device__ __forceinline__ uint32_t w(int i) const { return ws[i * 32 + lane]; }
-    __device__ __forceinline__ float b(int i) const { return bs[i * 32 + lane]; }
+    const uint32_t* ws;  // this lane's weight fragments
+    const float* bs;     // this lane's biases
+    __device__ __forceinline__ uint4 w4(int k) const {
+        return reinterpret_cast<const uint4*>(ws)[k];
+    }
+    __device__ __forceinline__ float4 b4(int k) const {
+        return reinterpret_cast<const float4*>(bs)[k];
+    }
+    // layer 1: weights w[0..3], biases b[0..7]
+    __device__ __forceinline__ void layer1(uint32_t* w, float* b) const {
+        const uint4 a = w4(0);
+        const float4 p = b4(0), q = b4(1);
+        w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
+        b[0] = p.x; b[1] = p.y; b[2] = p.z; b[3] = p.w;
+        b[4] = q.x; b[5] = q.y; b[6] = q.z; b[7] = q.w;
+    }
+    // layer 2: weights w[4..19] (as w[0..15]), biases b[8..15] (as b[0..7])
+    __device__ __forceinline__ void layer2(uint32_t* w, float* b) const {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint4 a = w4(1 + k);
+            w[4 * k] = a.x; w[4 * k + 1] = a.y; w[4 * k + 2] = a.z; w[4 * k + 3] = a.w;
+        }
+        const float4 p = b4(2), q = b4(3);
+        b[0] = p.x; b[1] = p.y; b[2] = p.z; b[3] = p.w;
+        b[4] = q.x; b[5] = q.y; b[6] = q.z; b[7] = q.w;
+    }
+    // layer 3: weights w[20..23] (as w[0..3]), bias b[16]
+    __device__ __forceinline__ void layer3(uint32_t* w, float& b) const {
+        const uint4 a = w4(5);
+        w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
+        b = b4(4).x;
+    }
 };
 
 __device__ void load_frags(const float* __restrict__ P, int lane, uint32_t* w, float* b,
@@ -176,47 +243,52 @@ __device__ float mlp16(const __nv_bfloat16* __restrict__ feat, int lane, const F
     const int g = lane >> 2, t = lane & 3;
     const uint32_t* row = reinterpret_cast<const uint32_t*>(feat);  // 8 u32 per row
     const uint32_t a0 = row[g * 8 + t], a1 = row[(g + 8) * 8 + t];
+    uint32_t w1[4], w2[16], w3[4];
+    float b1[8], b2[8], b3;
+    F.layer1(w1, b1);
     float c1[4][4];
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt) {
-        c1[nt][0] = F.b(nt * 2 + 0);
-        c1[nt][1] = F.b(nt * 2 + 1);
-        c1[nt][2] = F.b(nt * 2 + 0);
-        c1[nt][3] = F.b(nt * 2 + 1);
-        mma16816(c1[nt], a0, a1, 0u, 0u, F.w(nt), 0u);
+        c1[nt][0] = b1[nt * 2 + 0];
+        c1[nt][1] = b1[nt * 2 + 1];
+        c1[nt][2] = b1[nt * 2 + 0];
+        c1[nt][3] = b1[nt * 2 + 1];
+        mma16816(c1[nt], a0, a1, 0u, 0u, w1[nt], 0u);
     }
+    F.layer2(w2, b2);
     uint32_t h1[2][4];
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks) {
-        h1[ks][0] = pack_bf16(fmaxf(c1[2 * ks][0], 0.f), fmaxf(c1[2 * ks][1], 0.f));
-        h1[ks][1] = pack_bf16(fmaxf(c1[2 * ks][2], 0.f), fmaxf(c1[2 * ks][3], 0.f));
-        h1[ks][2] = pack_bf16(fmaxf(c1[2 * ks + 1][0], 0.f), fmaxf(c1[2 * ks + 1][1], 0.f));
-        h1[ks][3] = pack_bf16(fmaxf(c1[2 * ks + 1][2], 0.f), fmaxf(c1[2 * ks + 1][3], 0.f));
+        h1[ks][0] = pack_bf16_relu(c1[2 * ks][0], c1[2 * ks][1]);
+        h1[ks][1] = pack_bf16_relu(c1[2 * ks][2], c1[2 * ks][3]);
+        h1[ks][2] = pack_bf16_relu(c1[2 * ks + 1][0], c1[2 * ks + 1][1]);
+        h1[ks][3] = pack_bf16_relu(c1[2 * ks + 1][2], c1[2 * ks + 1][3]);
     }
     float c2[4][4];
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt) {
-        c2[nt][0] = F.b(8 + nt * 2 + 0);
-        c2[nt][1] = F.b(8 + nt * 2 + 1);
-        c2[nt][2] = F.b(8 + nt * 2 + 0);
-        c2[nt][3] = F.b(8 + nt * 2 + 1);
+        c2[nt][0] = b2[nt * 2 + 0];
+        c2[nt][1] = b2[nt * 2 + 1];
+        c2[nt][2] = b2[nt * 2 + 0];
+        c2[nt][3] = b2[nt * 2 + 1];
 #pragma unroll
         for (int ks = 0; ks < 2; ++ks)
-            mma16816(c2[nt], h1[ks][0], h1[ks][1], h1[ks][2], h1[ks][3], F.w(4 + (ks * 4 + nt) * 2 + 0),
-                     F.w(4 + (ks * 4 + nt) * 2 + 1));
+            mma16816(c2[nt], h1[ks][0], h1[ks][1], h1[ks][2], h1[ks][3], w2[(ks * 4 + nt) * 2],
+                     w2[(ks * 4 + nt) * 2 + 1]);
     }
+    F.layer3(w3, b3);
     uint32_t h2[2][4];
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks) {
-        h2[ks][0] = pack_bf16(fmaxf(c2[2 * ks][0], 0.f), fmaxf(c2[2 * ks][1], 0.f));
-        h2[ks][1] = pack_bf16(fmaxf(c2[2 * ks][2], 0.f), fmaxf(c2[2 * ks][3], 0.f));
-        h2[ks][2] = pack_bf16(fmaxf(c2[2 * ks + 1][0], 0.f), fmaxf(c2[2 * ks + 1][1], 0.f));
-        h2[ks][3] = pack_bf16(fmaxf(c2[2 * ks + 1][2], 0.f), fmaxf(c2[2 * ks + 1][3], 0.f));
+        h2[ks][0] = pack_bf16_relu(c2[2 * ks][0], c2[2 * ks][1]);
+        h2[ks][1] = pack_bf16_relu(c2[2 * ks][2], c2[2 * ks][3]);
+        h2[ks][2] = pack_bf16_relu(c2[2 * ks + 1][0], c2[2 * ks + 1][1]);
+        h2[ks][3] = pack_bf16_relu(c2[2 * ks + 1][2], c2[2 * ks + 1][3]);
     }
-    float c3[4] = {F.b(16), F.b(16), F.b(16), F.b(16)};
+    float c3[4] = {b3, b3, b3, b3};
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks)
-        mma16816(c3, h2[ks][0], h2[ks][1], h2[ks][2], h2[ks][3], F.w(20 + ks * 2 + 0), F.w(20 + ks * 2 + 1));
+        mma16816(c3, h2[ks][0], h2[ks][1], h2[ks][2], h2[ks][3], w3[ks * 2], w3[ks * 2 + 1]);
     // row r's score sits in lane 4*(r%8): c3[0] for r < 8, c3[2] for r >= 8
     const int r = lane & 15;
     const float v0 = __shfl_sync(0xffffffffu, c3[0], 4 * (r & 7));
@@ -237,36 +309,40 @@ __device__ float mlp32(const __nv_bfloat16* __restrict__ feat, int lane, const F
         a0[b] = row[(16 * b + g) * 8 + t];
         a1[b] = row[(16 * b + g + 8) * 8 + t];
     }
+    uint32_t w1[4], w2[16], w3[4];
+    float b1[8], b2[8], b3;
+    F.layer1(w1, b1);
     float c1[2][4][4];
 #pragma unroll
     for (int b = 0; b < 2; ++b)
 #pragma unroll
         for (int nt = 0; nt < 4; ++nt) {
-            c1[b][nt][0] = F.b(nt * 2 + 0);
-            c1[b][nt][1] = F.b(nt * 2 + 1);
-            c1[b][nt][2] = F.b(nt * 2 + 0);
-            c1[b][nt][3] = F.b(nt * 2 + 1);
-            mma16816(c1[b][nt], a0[b], a1[b], 0u, 0u, F.w(nt), 0u);
+            c1[b][nt][0] = b1[nt * 2 + 0];
+            c1[b][nt][1] = b1[nt * 2 + 1];
+            c1[b][nt][2] = b1[nt * 2 + 0];
+            c1[b][nt][3] = b1[nt * 2 + 1];
+            mma16816(c1[b][nt], a0[b], a1[b], 0u, 0u, w1[nt], 0u);
         }
+    F.layer2(w2, b2);
     uint32_t h[2][2][4];
 #pragma unroll
     for (int b = 0; b < 2; ++b)
 #pragma unroll
         for (int ks = 0; ks < 2; ++ks) {
-            h[b][ks][0] = pack_bf16(fmaxf(c1[b][2 * ks][0], 0.f), fmaxf(c1[b][2 * ks][1], 0.f));
-            h[b][ks][1] = pack_bf16(fmaxf(c1[b][2 * ks][2], 0.f), fmaxf(c1[b][2 * ks][3], 0.f));
-            h[b][ks][2] = pack_bf16(fmaxf(c1[b][2 * ks + 1][0], 0.f), fmaxf(c1[b][2 * ks + 1][1], 0.f));
-            h[b][ks][3] = pack_bf16(fmaxf(c1[b][2 * ks + 1][2], 0.f), fmaxf(c1[b][2 * ks + 1][3], 0.f));
+            h[b][ks][0] = pack_bf16_relu(c1[b][2 * ks][0], c1[b][2 * ks][1]);
+            h[b][ks][1] = pack_bf16_relu(c1[b][2 * ks][2], c1[b][2 * ks][3]);
+            h[b][ks][2] = pack_bf16_relu(c1[b][2 * ks + 1][0], c1[b][2 * ks + 1][1]);
+            h[b][ks][3] = pack_bf16_relu(c1[b][2 * ks + 1][2], c1[b][2 * ks + 1][3]);
         }
     float c2[2][4][4];
 #pragma unroll
     for (int b = 0; b < 2; ++b)
 #pragma unroll
         for (int nt = 0; nt < 4; ++nt) {
-            c2[b][nt][0] = F.b(8 + nt * 2 + 0);
-            c2[b][nt][1] = F.b(8 + nt * 2 + 1);
-            c2[b][nt][2] = F.b(8 + nt * 2 + 0);
-            c2[b][nt][3] = F.b(8 + nt * 2 + 1);
+            c2[b][nt][0] = b2[nt * 2 + 0];
+            c2[b][nt][1] = b2[nt * 2 + 1];
+            c2[b][nt][2] = b2[nt * 2 + 0];
+            c2[b][nt][3] = b2[nt * 2 + 1];
         }
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks)
@@ -275,27 +351,27 @@ __device__ float mlp32(const __nv_bfloat16* __restrict__ feat, int lane, const F
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt)
                 mma16816(c2[b][nt], h[b][ks][0], h[b][ks][1], h[b][ks][2], h[b][ks][3],
-                         F.w(4 + (ks * 4 + nt) * 2 + 0), F.w(4 + (ks * 4 + nt) * 2 + 1));
+                         w2[(ks * 4 + nt) * 2], w2[(ks * 4 + nt) * 2 + 1]);
+    F.layer3(w3, b3);
 #pragma unroll
     for (int b = 0; b < 2; ++b)
 #pragma unroll
         for (int ks = 0; ks < 2; ++ks) {
-            h[b][ks][0] = pack_bf16(fmaxf(c2[b][2 * ks][0], 0.f), fmaxf(c2[b][2 * ks][1], 0.f));
-            h[b][ks][1] = pack_bf16(fmaxf(c2[b][2 * ks][2], 0.f), fmaxf(c2[b][2 * ks][3], 0.f));
-            h[b][ks][2] = pack_bf16(fmaxf(c2[b][2 * ks + 1][0], 0.f), fmaxf(c2[b][2 * ks + 1][1], 0.f));
-            h[b][ks][3] = pack_bf16(fmaxf(c2[b][2 * ks + 1][2], 0.f), fmaxf(c2[b][2 * ks + 1][3], 0.f));
+            h[b][ks][0] = pack_bf16_relu(c2[b][2 * ks][0], c2[b][2 * ks][1]);
+            h[b][ks][1] = pack_bf16_relu(c2[b][2 * ks][2], c2[b][2 * ks][3]);
+            h[b][ks][2] = pack_bf16_relu(c2[b][2 * ks + 1][0], c2[b][2 * ks + 1][1]);
+            h[b][ks][3] = pack_bf16_relu(c2[b][2 * ks + 1][2], c2[b][2 * ks + 1][3]);
         }
     float c3[2][4];
 #pragma unroll
     for (int b = 0; b < 2; ++b) {
-        c3[b][0] = c3[b][1] = c3[b][2] = c3[b][3] = F.b(16);
+        c3[b][0] = c3[b][1] = c3[b][2] = c3[b][3] = b3;
     }
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks)
 #pragma unroll
         for (int b = 0; b < 2; ++b)
-            mma16816(c3[b], h[b][ks][0], h[b][ks][1], h[b][ks][2], h[b][ks][3], F.w(20 + ks * 2 + 0),
-                     F.w(20 + ks * 2 + 1));
+            mma16816(c3[b], h[b][ks][0], h[b][ks][1], h[b][ks][2], h[b][ks][3], w3[ks * 2], w3[ks * 2 + 1]);
     // row r of block b sits in lane 4*(r%8): c3[b][0] for r < 8, c3[b][2] for r >= 8
     const int r = lane & 15, src = 4 * (r & 7);
     const float v00 = __shfl_sync(0xffffffffu, c3[0][0], src);
@@ -368,17 +444,20 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
                   float theta2, uint32_t count_cap, float eps2, const uint32_t* __restrict__ ids,
                   double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az,
                   unsigned long long* __restrict__ counters, uint32_t* __restrict__ err_word,
-                  uint32_t* __restrict__ next_group, int cap) {
+                  uint32_t* __restrict__ next_group, int cap, const double* __restrict__ box) {
     // cap <= LT_CAP: the stack entries a walk may use (LT_CAP except in the failure-path tests)
     __shared__ uint32_t stack[LT_WARPS][LT_CAP];
     __shared__ __align__(16) __nv_bfloat16 feat[LT_WARPS][LT_BATCH][16];
     // the group's positions as packed pairs (bodies 2j, 2j+1) per axis, for the gap loop
     __shared__ nb_f2 gpx[LT_WARPS][16], gpy[LT_WARPS][16], gpz[LT_WARPS][16];
     __shared__ float4 ilist[LT_WARPS][LT_LIST];
-    __shared__ uint32_t wfrag[MF_W * 32];
-    __shared__ float bfrag[MF_B * 32];
+    __shared__ __align__(16) uint32_t wfrag[32 * MF_WS];
+    __shared__ __align__(16) float bfrag[32 * MF_BS];
+    __shared__ BoxScale bs;  // in shared memory: no registers held through the walk
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
-    if (params != nullptr && wi == 0) load_frags(params, lane, wfrag + lane, bfrag + lane, 32);
+    if (threadIdx.x == 0) bs = BoxScale(box[6]);
+    if (params != nullptr && wi == 0)
+        load_frags(params, lane, wfrag + lane * MF_WS, bfrag + lane * MF_BS, 1);
     __syncthreads();  // before any warp leaves
     const uint32_t n_groups = (n + 31) / 32;
     unsigned long long t_acc = 0, t_mlp = 0, t_cells = 0, t_steps = 0;
@@ -413,7 +492,7 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
         reinterpret_cast<float*>(gpy[wi])[lane] = valid ? ph.y : inf;
         reinterpret_cast<float*>(gpz[wi])[lane] = valid ? ph.z : inf;
         const bool use_net = params != nullptr;
-        const MlpFragsSmem F{wfrag, bfrag, lane};
+        const MlpFragsSmem F{wfrag + lane * MF_WS, bfrag + lane * MF_BS};
         uint32_t* st = stack[wi];
         __nv_bfloat16* fm = &feat[wi][0][0];
         for (int k = lane; k < LT_BATCH * 16; k += 32) fm[k] = __float2bfloat16(0.f);
@@ -470,14 +549,17 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
                     m2 = fminf(m2, fminf(d0, d1));
                 }
             }
-            const float gap = sqrtf(m2);
             int cls = 1;
             uint4 fv = make_uint4(0u, 0u, 0u, 0u);  // the features as BF16 pairs
             if (live) {
-                float f[NF];
-                cls = cell_features(r, xa, G, gap, count_cap, f, bound_tau);
-                fv = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]),
-                                pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+                if (use_net) {
+                    float f[NF];
+                    cls = cell_features(r, xa, G, bs, m2, count_cap, f, bound_tau);
+                    fv = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]),
+                                    pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+                } else {  // the theta rule needs the class only
+                    cls = cell_class(r, xa, m2, count_cap);
+                }
             }
             // the network's cells are packed into the first rows of the feature tile
             const unsigned net_mask = __ballot_sync(0xffffffffu, live && cls == 0);
@@ -497,7 +579,7 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
                 if (cls == 1 || cls == 4) accept = true;
                 else if (cls == 0 && use_net) accept = score < log_tau_scaled;
                 else if (cls != 2)  // group theta rule on the smallest distance
-                    accept = gap > 0.f && r.edge2 < theta2 * gap * gap;
+                    accept = m2 > 0.f && r.edge2 < theta2 * m2;
             }
             // body leaves and small opened cells: their bodies; other accepted cells: the monopole
             const bool body_leaf = live && cls == 1;
@@ -633,14 +715,13 @@ pairs_collect_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restric
             continue;
         }
         const NodeAux xa = aux[k];
-        const float gap = warp_min_dist(valid, px, py, pz, r.cx, r.cy, r.cz);
-        float f[NF];
-        const int cls = cell_features(r, xa, G, gap, count_cap, f);
+        const float m2 = warp_min_dist2(valid, px, py, pz, r.cx, r.cy, r.cz);
+        const int cls = cell_class(r, xa, m2, count_cap);
         if (cls == 0 && lane == 0 && hash32(k * 2654435761u ^ gw ^ seed) < threshold) {
             const unsigned int slot = atomicAdd(counter, 1u);
             if (slot < max_pairs) out[slot] = make_uint2(gw, k);
         }
-        const bool open = cls == 2 || !(gap > 0 && r.edge2 < theta2 * gap * gap);
+        const bool open = cls == 2 || !(m2 > 0 && r.edge2 < theta2 * m2);
         k = open ? k + 1 : r.skip;
     }
 }
@@ -679,9 +760,9 @@ pairs_label_kernel(const NodeRec32* __restrict__ rec, const NodeRec64* __restric
         const GroupGeo Gg = group_geo(valid, px, py, pz, a_b);
         const NodeRec32 r = rec[pr.y];
         const NodeAux xa = aux[pr.y];
-        const float gap = warp_min_dist(valid, px, py, pz, r.cx, r.cy, r.cz);
+        const float m2 = warp_min_dist2(valid, px, py, pz, r.cx, r.cy, r.cz);
         float f[NF];
-        cell_features(r, xa, Gg, gap, count_cap, f);
+        cell_features(r, xa, Gg, BoxScale(box[6]), m2, count_cap, f);
         // exact cell force on each lane's body; positions relative to the group's first valid
         // body in FP64 before rounding, so close pairs keep their digits
         const double gx = __shfl_sync(0xffffffffu, bx, 0), gy = __shfl_sync(0xffffffffu, by, 0),
@@ -860,12 +941,12 @@ __global__ void __launch_bounds__(128)
 mlp_predict_bf16_kernel(const float* __restrict__ P, const float* __restrict__ X, uint32_t n,
                         float* __restrict__ out) {
     __shared__ __align__(16) __nv_bfloat16 feat[4][32][16];
-    __shared__ uint32_t wsm[MF_W * 32];
-    __shared__ float bsm[MF_B * 32];
+    __shared__ __align__(16) uint32_t wsm[32 * MF_WS];
+    __shared__ __align__(16) float bsm[32 * MF_BS];
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
-    if (wi == 0) load_frags(P, lane, wsm + lane, bsm + lane, 32);
+    if (wi == 0) load_frags(P, lane, wsm + lane * MF_WS, bsm + lane * MF_BS, 1);
     __syncthreads();
-    const MlpFragsSmem F{wsm, bsm, lane};
+    const MlpFragsSmem F{wsm + lane * MF_WS, bsm + lane * MF_BS};
     __nv_bfloat16* fm = &feat[wi][0][0];
     for (uint32_t base = (blockIdx.x * 4 + wi) * 32; base < n; base += gridDim.x * 4 * 32) {
         for (int k = lane; k < 512; k += 32) {
@@ -1017,7 +1098,7 @@ nb_status launch_learned(nb_ctx* ctx, const nb_bh_tree* t, const double* x, cons
         (t->policy_flags & NB_POLICY_BOUND_ACCEPT) ? exp10f(t->policy_log_tau) : 0.f,
         t->policy_theta * t->policy_theta, t->policy_count_cap,
         (float)eps2, t->ids, ax, ay, az, counters, ctx->dev_error, t->work,
-        ctx->learned_stack_cap ? (int)ctx->learned_stack_cap : LT_CAP);
+        ctx->learned_stack_cap ? (int)ctx->learned_stack_cap : LT_CAP, t->box);
     return check_launch("bh_learned_kernel");
 }
 

@@ -107,12 +107,12 @@ scan_apply_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, u
 // depend on the counts only.
 // ---------------------------------------------------------------------------------------------
 constexpr int RS_THREADS = 256;
-constexpr int RS_ITEMS = 8;
+constexpr int RS_ITEMS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_BINS = 256;
 constexpr int RS_MAX_PASSES = 8;
-// look-back words: 2 flag bits over a 30-bit count (tile counts <= 2048, totals <= n < 2^30)
+// look-back words: 2 flag bits over a 30-bit count (tile counts <= 4096, totals <= n < 2^30)
 constexpr uint32_t LB_AGGREGATE = 1u << 30;
 constexpr uint32_t LB_TOTAL = 2u << 30;
 constexpr uint32_t LB_VALUE = (1u << 30) - 1u;
@@ -137,14 +137,11 @@ radix_hist_all_kernel(const uint64_t* __restrict__ keys, uint32_t n, int begin_b
     }
 }
 
-// hist[p][d] -> exclusive prefix over d (one block, thread d).
-__global__ void __launch_bounds__(RS_BINS) radix_offsets_kernel(uint32_t* __restrict__ hist,
-                                                                int passes) {
-    for (int p = 0; p < passes; ++p) {
-        uint32_t total;
-        const uint32_t ex = block_exclusive_scan(hist[p * RS_BINS + threadIdx.x], &total);
-        hist[p * RS_BINS + threadIdx.x] = ex;
-    }
+// hist[p][d] -> exclusive prefix over d (block p, thread d).
+__global__ void __launch_bounds__(RS_BINS) radix_offsets_kernel(uint32_t* __restrict__ hist) {
+    uint32_t total;
+    uint32_t* h = hist + blockIdx.x * RS_BINS;
+    h[threadIdx.x] = block_exclusive_scan(h[threadIdx.x], &total);
 }
 
 __device__ __forceinline__ void lb_store(uint32_t* p, uint32_t v) {
@@ -155,6 +152,9 @@ __device__ __forceinline__ uint32_t lb_load(const uint32_t* p) {
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+
+// The tile's keys and values reordered by digit (dynamic shared memory: above the static limit).
+constexpr int RS_REORDER_BYTES = RS_TILE * (int)(sizeof(uint64_t) + sizeof(uint32_t));
 
 // One digit pass: keys of tile `ticket` in, ranked within the tile (warp-striped, stable),
 // placed at digit offset + keys of the digit in earlier tiles + rank.
@@ -167,15 +167,16 @@ radix_pass_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __restri
     __shared__ uint32_t wcnt[RS_WARPS][RS_BINS];
     __shared__ uint32_t tile_base[RS_BINS];   // first output position of the tile's digit d
     __shared__ uint32_t digit_local[RS_BINS];  // first tile position of digit d after the reorder
-    __shared__ uint64_t skeys[RS_TILE];
-    __shared__ uint32_t svals[RS_TILE];
+    extern __shared__ __align__(16) unsigned char rs_reorder[];  // RS_REORDER_BYTES
+    uint64_t* skeys = reinterpret_cast<uint64_t*>(rs_reorder);
+    uint32_t* svals = reinterpret_cast<uint32_t*>(rs_reorder + RS_TILE * sizeof(uint64_t));
     __shared__ uint32_t tile_s;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) tile_s = atomicAdd(ticket, 1u);
     for (int b = threadIdx.x; b < RS_WARPS * RS_BINS; b += RS_THREADS) (&wcnt[0][0])[b] = 0;
     __syncthreads();
     const uint32_t tile = tile_s;
-    // warp-striped: warp w owns tile positions [w*256, w*256+256); item k, lane l -> w*256+k*32+l
+    // warp-striped: warp w owns tile positions [w*512, w*512+512); item k, lane l -> w*512+k*32+l
     const uint32_t base = tile * RS_TILE + warp * (RS_ITEMS * 32);
     uint64_t key[RS_ITEMS];
     uint32_t val[RS_ITEMS], digit[RS_ITEMS], rank[RS_ITEMS];
@@ -297,6 +298,18 @@ nb_status exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int 
     return check_launch("scan_apply_kernel");
 }
 
+nb_status radix_prepare() {
+    static bool done[64] = {};
+    int dev = 0;
+    NB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || done[dev]) return NB_OK;
+    NB_CUDA_TRY(cudaFuncSetAttribute(radix_pass_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     RS_REORDER_BYTES));
+    done[dev] = true;
+    return NB_OK;
+}
+
 // Temporary storage of radix_sort_pairs: digit offsets and tickets of all passes, then one
 // look-back word per (pass, tile, digit).
 size_t radix_temp_bytes(uint32_t n) {
@@ -317,6 +330,7 @@ nb_status radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
     if (passes < 1 || passes > RS_MAX_PASSES)
         return set_error(NB_ERR_INVALID_ARG, "radix_sort_pairs: bit range [%d, %d)", begin_bit,
                          end_bit);
+    NB_TRY(radix_prepare());
     const uint32_t tiles = (n + RS_TILE - 1) / RS_TILE;
     uint32_t* offs = (uint32_t*)temp;                   // [passes][256]
     uint32_t* tickets = offs + RS_MAX_PASSES * RS_BINS;  // [passes]
@@ -325,7 +339,7 @@ nb_status radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
     const int hist_blocks = (int)std::min<uint32_t>(tiles, 1024u);
     radix_hist_all_kernel<<<hist_blocks, RS_THREADS, 0, stream>>>(keys, n, begin_bit, passes, offs);
     NB_TRY(check_launch("radix_hist_all_kernel"));
-    radix_offsets_kernel<<<1, RS_BINS, 0, stream>>>(offs, passes);
+    radix_offsets_kernel<<<passes, RS_BINS, 0, stream>>>(offs);
     NB_TRY(check_launch("radix_offsets_kernel"));
     uint64_t* kin = keys;
     uint32_t* vin = vals;
@@ -333,7 +347,7 @@ nb_status radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
     uint32_t* vout = vals_alt;
     int flips = 0;
     for (int p = 0; p < passes; ++p) {
-        radix_pass_kernel<<<tiles, RS_THREADS, 0, stream>>>(
+        radix_pass_kernel<<<tiles, RS_THREADS, RS_REORDER_BYTES, stream>>>(
             kin, vin, kout, vout, n, begin_bit + 8 * p, offs + p * RS_BINS,
             lb + (size_t)p * tiles * RS_BINS, tickets + p, err, wait_limit, drop_first);
         NB_TRY(check_launch("radix_pass_kernel"));

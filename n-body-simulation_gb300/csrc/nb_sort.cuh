@@ -11,6 +11,9 @@ nb_status exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, int 
                              uint32_t* temp, cudaStream_t stream);
 
 size_t radix_temp_bytes(uint32_t n);
+// One-time set-up of the sort's kernels on the current device (their dynamic shared memory);
+// radix_sort_pairs calls it, and so do callers that may sort inside a stream capture, earlier.
+nb_status radix_prepare();
 // Stable LSD sort of (keys, vals) on bits [begin_bit, end_bit) (at most 64) in 8-bit digits, one
 // launch per digit pass after one histogram launch, ping-ponging with (keys_alt, vals_alt);
 // *result_in_alt says which pair holds the result. A look-back wait that runs out (after

@@ -148,3 +148,37 @@ def test_trained_policy_gain_over_theta_walk(ctx):
           f"p99 {bl['p99']:.2e}, {bl['ms']:.3f} ms; theta-walk {bt['param']}: "
           f"{bt['interactions'] / n:.0f} interactions/body, p99 {bt['p99']:.2e}, {bt['ms']:.3f} ms")
     assert bl["interactions"] <= 0.8 * bt["interactions"]
+
+
+def test_trained_policy_holds_on_held_out_seeds(ctx):
+    """The gain holds on systems the threshold was not tuned on: tau is chosen once on a
+    validation mix (the cheapest setting within 1e-4 median / 1e-3 p99 relative force error
+    against FP64 naive sums), then on three held-out mixes the learned policy at that fixed tau
+    stays within the bounds and needs at most 0.8x the body-cell interactions of the same walk
+    with the group theta rule at each system's own cheapest theta within the bounds."""
+    from nbody import generators, learned
+    n = 65536
+    X, Y = learned.training_set(ctx, n, 400_000, seeds=(31, 32))
+    params, _ = learned.train(ctx, X, Y, epochs=3, batch=8192, lr=2e-3)
+    targets = learned.sample_targets(n, 4096)
+
+    def rows_for(seed, taus, thetas):
+        d = generators.disc_plummer_mix(n, seed=seed)
+        t = learned.device_system(d)
+        ref = learned.fp64_reference(ctx, t, d["G"], targets)
+        return learned.sweep(ctx, t, d["G"], targets, ref, params, taus=taus, thetas=thetas)
+
+    val = rows_for(40, (-5.0, -4.75, -4.5, -4.25, -4.0, -3.75), ())
+    chosen = learned.best_within(val, "learned", key="interactions")
+    assert chosen is not None, val
+    for seed in (41, 42, 43):
+        rows = rows_for(seed, (chosen["param"],), (0.25, 0.3, 0.35, 0.4, 0.45, 0.5))
+        lr = [r for r in rows if r["kind"] == "learned"][0]
+        bt = learned.best_within(rows, "theta-walk", key="interactions")
+        assert bt is not None, rows
+        print(f"\nseed {seed}: learned tau 1e{chosen['param']}: {lr['interactions'] / n:.0f} "
+              f"interactions/body, median {lr['median']:.1e} p99 {lr['p99']:.2e}, "
+              f"{lr['ms']:.3f} ms; theta-walk {bt['param']}: {bt['interactions'] / n:.0f}, "
+              f"{bt['ms']:.3f} ms")
+        assert lr["median"] <= 1e-4 and lr["p99"] <= 1e-3, lr
+        assert lr["interactions"] <= 0.8 * bt["interactions"], (lr, bt)
