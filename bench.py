@@ -382,7 +382,9 @@ def run_ours(args):
 
     also = {}
     if rank == 0 and ws == 1 and not args.quick:  # one GPU only: replicas runs stay short
-        also = secondary_measurements(ctx, tree, m, pos, acc, G)
+        also = secondary_measurements(ctx, tree, m, pos, acc, G,
+                                      with_cpu=not args.no_cpu_baseline,
+                                      bench_ms_per_step=ms_per_step)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline and not args.quick:
@@ -440,7 +442,109 @@ def run_ours(args):
     return 0
 
 
-def secondary_measurements(ctx, tree, m, pos, acc, G):
+def config1_cli_run(with_cpu: bool):
+    """The reference's CPU-path configuration end to end through the reference's surface: the
+    host driver nbody_sim, naive FP64 (opt_stage 2, block size 128) on the seeded 16,384-body
+    heliocentric disc written as the reference's CSV, dt = 1 h, t_end = 10 d (240 leapfrog steps
+    after the initial evaluation), energies on, output every 10 days. Wall time of the process
+    (CSV parsing, CUDA context, upload, the run, output files) and the device time of its phases
+    from its times.json; beside it the restated reference's full run of the same loop on the
+    host cores (OpenMP), as the baseline."""
+    import shutil
+    import tempfile
+
+    import numpy as np
+
+    from nbody import generators
+    exe = os.path.join(PKG, "_build", "nbody_sim")
+    d = generators.heliocentric_disc(16384, 1)
+    work = tempfile.mkdtemp(prefix="nbody_cfg1_")
+    try:
+        csv = os.path.join(work, "disc16384.csv")
+        generators.write_csv(csv, d)
+        out = os.path.join(work, "out")
+        cmd = [exe, f"--file={csv}", "--dt=1h", "--t_end=10d", "--vs=10d", f"--vs_dir={out}",
+               "--algorithm=naive", "--opt_stage=2", "--block_size=128", "--energy=true"]
+        t0 = time.perf_counter()
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        wall = time.perf_counter() - t0
+        if r.returncode != 0:
+            return {"error": r.stderr[-500:]}
+        run_dir = os.path.join(out, os.listdir(out)[0])
+        with open(os.path.join(run_dir, "times.json")) as f:
+            times = json.load(f)
+        res = {"command": "nbody_sim --file=disc16384.csv --dt=1h --t_end=10d --vs=10d "
+                          "--algorithm=naive --opt_stage=2 --block_size=128 --energy=true",
+               "steps": 240, "evaluations": 241, "cli_wall_s": wall,
+               "device_s": {k: sum(v) / 1e3 for k, v in times.items() if isinstance(v, list)},
+               "gpairs_per_s_over_wall": 241 * 16384.0 ** 2 / wall / 1e9}
+        if with_cpu:
+            import oracle
+            x, y, z = d["x"].copy(), d["y"].copy(), d["z"].copy()
+            v = [d["vx"].copy(), d["vy"].copy(), d["vz"].copy()]
+            t0 = time.perf_counter()
+            a = list(oracle.naive_accel(d["m"], x, y, z, d["G"], EPS2))
+            for _ in range(240):
+                vh = oracle.leapfrog_part1(v, [x, y, z], a, DT)
+                a = list(oracle.naive_accel(d["m"], x, y, z, d["G"], EPS2))
+                oracle.leapfrog_part2(v, vh, a, DT)
+            cpu = time.perf_counter() - t0
+            rows = np.loadtxt(os.path.join(run_dir, "lastState.csv"), delimiter=",", skiprows=1)
+            dev_ = max(float(np.max(np.abs(rows[:, c] - o) / (np.abs(o) + 1e-9)))
+                       for c, o in enumerate((x, y, z)))
+            res["cpu_baseline"] = {"kind": "port", "cores": os.cpu_count(), "run_s": cpu,
+                                   "sample": "the full run: 241 naive FP64 evaluations and 240 "
+                                             "leapfrog steps (restated reference, OpenMP)",
+                                   "speedup_cli_wall": cpu / wall}
+            res["last_state_max_rel_diff_vs_cpu"] = dev_
+        return res
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+def config2_cli_run(bench_ms_per_step: float, steps: int = 10):
+    """The headline configuration through the reference's surface: nbody_sim on the seeded
+    1,048,576-body disc written as the reference's CSV, Barnes-Hut FP64, theta = 0.5, dt = 1 h,
+    `steps` steps, output of the first and the last step only. The driver enqueues the whole run
+    on one stream and times its phases with CUDA events (times.json); the per-step sum of its
+    phases is compared with the bench's device-timed step."""
+    import shutil
+    import tempfile
+
+    from nbody import generators
+    exe = os.path.join(PKG, "_build", "nbody_sim")
+    d = generators.heliocentric_disc(N_BODIES, SEED)
+    work = tempfile.mkdtemp(prefix="nbody_cfg2_")
+    try:
+        csv = os.path.join(work, "disc.csv")
+        generators.write_csv(csv, d)
+        out = os.path.join(work, "out")
+        cmd = [exe, f"--file={csv}", "--dt=1h", f"--t_end={steps}h", f"--vs={steps}h",
+               f"--vs_dir={out}", "--algorithm=BarnesHut", f"--theta={THETA}"]
+        t0 = time.perf_counter()
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        wall = time.perf_counter() - t0
+        if r.returncode != 0:
+            return {"error": r.stderr[-500:]}
+        run_dir = os.path.join(out, os.listdir(out)[0])
+        with open(os.path.join(run_dir, "times.json")) as f:
+            t = json.load(f)
+        # steps after the initial evaluation: leapfrog part 1, build + traversal, part 2
+        per_step = [a + b + c for a, b, c in zip(t["Leapfrog Part 1"], t["Total Time"][1:],
+                                                  t["Leapfrog Part 2"])]
+        ms = sum(per_step) / len(per_step)
+        return {"command": f"nbody_sim --file=disc.csv --dt=1h --t_end={steps}h --vs={steps}h "
+                           f"--algorithm=BarnesHut --theta={THETA}",
+                "steps": len(per_step), "ms_per_step_device": ms,
+                "bench_ms_per_step": bench_ms_per_step,
+                "ratio_to_bench_step": ms / bench_ms_per_step, "process_wall_s": wall,
+                "note": "process wall time includes parsing the 1M-row CSV, the CUDA context and "
+                        "two ASCII .vtp files of 1M bodies"}
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+def secondary_measurements(ctx, tree, m, pos, acc, G, with_cpu=True, bench_ms_per_step=None):
     """The other workloads on the same GPU: the FP32-pair group-rule step on the headline state,
     the reference's CPU-path configuration (naive FP64, 16,384-body disc), and the precision,
     batched and learned forms of the method (nbody/workloads.py)."""
@@ -535,6 +639,11 @@ def secondary_measurements(ctx, tree, m, pos, acc, G):
         "kernel": "pair_sym_df_kernel (each unordered pair once, added to both bodies)",
         "ms_per_eval": ms, "gpairs_per_s": n * n / (ms * 1e-3) / 1e9,
         "arithmetic": "double-float (FP32 pairs) on the FP32 pipe, FP64-accurate to ~1e-14"}
+    if bench_ms_per_step:
+        out["config2_bh_cli_disc_1M_10_steps"] = config2_cli_run(bench_ms_per_step)
+    t0 = time.perf_counter()
+    out["config1_naive_cli_disc_16384_10d"] = config1_cli_run(with_cpu)
+    out["config1_naive_cli_disc_16384_10d"]["bench_wall_s"] = time.perf_counter() - t0
     for name, fn in (("precision_form_naive_f32c_plummer_262144", workloads.precision_form),
                      ("batched_ensemble_512_plummer", workloads.batched_ensemble),
                      ("learned_opening_bh_mix_1M", workloads.learned_form)):
