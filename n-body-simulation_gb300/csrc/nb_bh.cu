@@ -18,8 +18,6 @@
 //     positions (deepest level first), cells reaching past their chunk by the last child to
 //     arrive; children summed in octant order 0..7 (bit-identical to
 //     BarnesHutOctree.cpp:304-311), node records written with the sums.
-#include <cuda/atomic>
-
 #include <algorithm>
 
 #include "nb_bh.cuh"
@@ -356,7 +354,7 @@ __global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
                             const uint32_t* __restrict__ base, uint8_t* __restrict__ node_level,
                             uint32_t* __restrict__ node_first, uint32_t* __restrict__ node_last,
                             uint32_t* __restrict__ node_skip, uint32_t* __restrict__ node_parent,
-                            uint32_t* __restrict__ node_body, uint32_t* __restrict__ node_nchild,
+                            uint32_t* __restrict__ node_body,
                             uint32_t* __restrict__ info, const uint64_t* __restrict__ key0,
                             const uint64_t* __restrict__ key1, uint32_t* __restrict__ children) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -374,7 +372,6 @@ __global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
         const uint32_t par = parent_of(p, p, dl, dr, split_level, split_start, base, mask);
         node_parent[idx] = par;
         if (par != NB_NONE) {
-            atomicAdd(&node_nchild[par], 1u);
             // the parent's level is the deeper boundary split; slot = visit rank there
             children[(size_t)par * 8 + digit_at(key0, key1, p, max(dl, dr))] = idx;
         }
@@ -393,7 +390,6 @@ __global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
         const uint32_t par = parent_of(a, b, dl, dr, split_level, split_start, base, mask);
         node_parent[idx] = par;
         if (par != NB_NONE) {
-            atomicAdd(&node_nchild[par], 1u);
             children[(size_t)par * 8 + digit_at(key0, key1, a, max(dl, dr))] = idx;
         }
     }
@@ -402,6 +398,7 @@ __global__ void emit_kernel(uint32_t n, const uint32_t* __restrict__ ids,
 struct ComArgs {
     uint32_t n;
     uint32_t* err;  // device error word
+
     uint32_t records;  // NB_REC_* sets to compute
     const double *m, *x, *y, *z;
     const double* box;
@@ -411,8 +408,8 @@ struct ComArgs {
     const unsigned long long* mask;
     const uint32_t* base;
     const uint8_t* node_level;
-    const uint32_t *node_first, *node_last, *node_skip, *node_parent, *node_body, *node_nchild;
-    uint32_t *node_arrive, *node_count;
+    const uint32_t *node_first, *node_last, *node_skip, *node_parent, *node_body;
+    uint32_t* node_count;
     double *comx, *comy, *comz, *mass, *q;
     NodeRec64* rec64;
     NodeRec32* rec32;
@@ -542,6 +539,25 @@ __device__ void sum_children(const ComArgs& A, uint32_t idx, bool records) {
     uint4* cl = reinterpret_cast<uint4*>(A.children + (size_t)idx * 8);
     const uint4 c0 = __ldcg(cl), c1 = __ldcg(cl + 1);
     const uint32_t vs[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+    const bool learned = (A.records & NB_REC_LEARNED) != 0;
+    // every child's sums requested before the first is used (one round trip, not eight)
+    double cx[8], cy[8], cz[8], cm[8], cq[8];
+    uint32_t cc[8];
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {  // the reference's octant order 0..7
+        const uint32_t ch = vs[nb_visit_of_octant(o)];
+        cx[o] = cy[o] = cz[o] = cm[o] = cq[o] = 0.0;
+        cc[o] = 0;
+        if (ch != NB_NONE) {
+            cx[o] = __ldcg(&A.comx[ch]);
+            cy[o] = __ldcg(&A.comy[ch]);
+            cz[o] = __ldcg(&A.comz[ch]);
+            cm[o] = __ldcg(&A.mass[ch]);
+            if (learned) cq[o] = __ldcg(&A.q[ch]);
+            cc[o] = __ldcg(&A.node_count[ch]);
+        }
+    }
+    // the compacted visit-order child list the learned traversal reads
     uint32_t list[8];
     int nch = 0;
 #pragma unroll
@@ -551,19 +567,17 @@ __device__ void sum_children(const ComArgs& A, uint32_t idx, bool records) {
     }
     cl[0] = make_uint4(list[0], list[1], list[2], list[3]);
     cl[1] = make_uint4(list[4], list[5], list[6], list[7]);
-    const bool learned = (A.records & NB_REC_LEARNED) != 0;
     double sx = 0, sy = 0, sz = 0, sm = 0, sq = 0;
     uint32_t count = 0;
 #pragma unroll
     for (int o = 0; o < 8; ++o) {
-        const uint32_t ch = vs[nb_visit_of_octant(o)];
-        if (ch == NB_NONE) continue;
-        sx = __dadd_rn(sx, __ldcg(&A.comx[ch]));
-        sy = __dadd_rn(sy, __ldcg(&A.comy[ch]));
-        sz = __dadd_rn(sz, __ldcg(&A.comz[ch]));
-        sm = __dadd_rn(sm, __ldcg(&A.mass[ch]));
-        if (learned) sq += __ldcg(&A.q[ch]);
-        count += __ldcg(&A.node_count[ch]);
+        if (vs[nb_visit_of_octant(o)] == NB_NONE) continue;  // absent children add nothing
+        sx = __dadd_rn(sx, cx[o]);
+        sy = __dadd_rn(sy, cy[o]);
+        sz = __dadd_rn(sz, cz[o]);
+        sm = __dadd_rn(sm, cm[o]);
+        if (learned) sq += cq[o];
+        count += cc[o];
     }
     A.comx[idx] = sx;
     A.comy[idx] = sy;
@@ -658,69 +672,41 @@ __device__ void leaf_sums(const ComArgs& A, uint32_t idx, uint32_t p, uint32_t b
     }
 }
 
-// A node whose sums are final arrives at its parent; the last child to arrive sums the parent
-// and climbs on. The acquire-release arrival publishes this thread's sums and, for the last
-// child, makes the siblings' sums visible. Parents have smaller DFS indices, so the climb ends;
-// it is also capped at the tree's depth.
-__device__ void arrive_and_climb(const ComArgs& A, uint32_t idx) {
-    uint32_t cur = A.node_parent[idx];
-    for (int guard = 0; cur != NB_NONE; ++guard) {
-        if (guard > 2 * NB_KEY_LEVELS + 2) {
-            atomicOr(A.err, NB_DEVERR_DEPTH);
-            return;
-        }
-        cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrive(A.node_arrive[cur]);
-        if (arrive.fetch_add(1u, cuda::memory_order_acq_rel) != A.node_nchild[cur] - 1u) return;
-        sum_children(A, cur, true);
-        cur = A.node_parent[cur];
-    }
-}
-
 // Centre of mass and records, bottom-up, in chunks of CW consecutive sorted positions. The nodes
 // starting in a chunk are the DFS indices [base[P], base[P + CW]); the ones that also end in it
-// ("local": all leaves and most cells) are summed without atomics, the few cells that reach past
-// their chunk ("global": the ancestors of chunk boundaries) by the arrival climb, which the local
-// nodes whose parent is global start.
-//  * com_leaf_kernel: one thread per sorted position sums its leaf and writes its records (and
-//    the leaf arrives at a global parent);
-//  * com_cells_kernel: one block per chunk sums the chunk's local cells level by level, deepest
-//    first (their children are leaves or deeper local cells), then writes their records in one
-//    sweep over the compacted cell list. FP64 work runs with full warps there: on this part an
-//    FP64 warp instruction costs the FP64 pipe the same time however few of its lanes are active,
-//    so the records stay out of the per-level rounds, where few lanes have a cell.
-constexpr int CW = 2048;                          // sorted positions per chunk
+// ("local": all leaves and most cells) are summed by the chunk's block. A cell that starts in a
+// chunk and reaches past its end holds the chunk's last body and the next one, so there is at
+// most one such cell per level: each chunk lists them (<= CM_LEVELS) for the next tier, whose
+// blocks cover CM_FAN chunks each and sum the listed cells that end inside their span, passing
+// the rest up again, until one block spans all bodies. Every sum has its children's sums final
+// before it starts (kernel order, then levels deepest first within a block), so no thread waits
+// on another, and the FP64 work is spread over all SMs at every tier.
+//  * com_leaf_kernel: one thread per sorted position sums its leaf and writes its records;
+//  * com_cells_kernel: one block per chunk sums the chunk's local cells level by level, then
+//    writes their records in one sweep over the compacted cell list (FP64 work with full warps:
+//    on this part an FP64 warp instruction costs the FP64 pipe the same time however few of its
+//    lanes are active);
+//  * com_tier_kernel: one block per span of CM_FAN lower-tier chunks, same scheme on the listed
+//    cells.
+constexpr int CW = 4096;                          // sorted positions per chunk
 constexpr int CM_LEVELS = 2 * NB_KEY_LEVELS + 1;  // node levels 0..42
-constexpr int CC_THREADS = 256;                   // threads per block of com_cells_kernel
-constexpr int CC_ROOTS = 512;                     // deferred arrivals kept per chunk
+constexpr int CM_FAN = 64;                        // lower-tier chunks per upper-tier chunk
+constexpr int CM_TIER_MAX = CM_LEVELS * CM_FAN;   // listed cells one upper-tier block reads
+constexpr int CM_TIERS = 5;                       // 2048 * 64^4 > 2^27 bodies
+constexpr int CC_THREADS = 256;                   // threads per block of the cell kernels
+constexpr int CC_BATCH = 4;  // node-table entries each thread loads together in the scan
 
 __global__ void __launch_bounds__(256, 5) com_leaf_kernel(ComArgs A) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= A.n) return;
-    const uint32_t idx = A.base[p] + __popcll(A.mask[p]);
-    leaf_sums(A, idx, p, A.ids[p]);
-    const uint32_t par = A.node_parent[idx];
-    if (par == NB_NONE) return;
-    const uint32_t c0 = p / CW * CW, c1 = min(c0 + (uint32_t)CW, A.n);
-    if (A.node_first[par] >= c0 && A.node_last[par] < c1) return;  // summed by its chunk's block
-    arrive_and_climb(A, idx);
+    leaf_sums(A, A.base[p] + __popcll(A.mask[p]), p, A.ids[p]);
 }
 
-__global__ void __launch_bounds__(CC_THREADS) com_cells_kernel(ComArgs A) {
-    __shared__ uint32_t nodes[CW];  // the chunk's local cells, grouped by level
-    __shared__ uint32_t cnt[CM_LEVELS], off[CM_LEVELS], fill[CM_LEVELS];
-    __shared__ uint2 roots[CC_ROOTS];  // (node, thread that summed it)
-    __shared__ uint32_t n_roots;
-    const uint32_t P = blockIdx.x * CW;
-    if (P >= A.n) return;
-    const uint32_t Pend = min(P + (uint32_t)CW, A.n);
-    const uint32_t d0 = A.base[P], d1 = A.base[Pend];
-    for (int l = threadIdx.x; l < CM_LEVELS; l += CC_THREADS) cnt[l] = fill[l] = 0;
-    if (threadIdx.x == 0) n_roots = 0;
-    __syncthreads();
-    for (uint32_t idx = d0 + threadIdx.x; idx < d1; idx += CC_THREADS)
-        if (A.node_body[idx] == NB_NONE && A.node_last[idx] < Pend)
-            atomicAdd(&cnt[min((int)A.node_level[idx], CM_LEVELS - 1)], 1u);
-    __syncthreads();
+// Sums the `nf` cells found[k] (level flev[k]) level by level, deepest first, then writes their
+// records. Block-wide; smem arrays given by the caller.
+__device__ void sum_by_level(const ComArgs& A, const uint32_t* found, const uint8_t* flev,
+                             uint32_t nf, uint32_t* nodes, uint32_t* cnt, uint32_t* off,
+                             uint32_t* fill) {
     if (threadIdx.x == 0) {
         uint32_t run = 0;
         for (int l = 0; l < CM_LEVELS; ++l) {
@@ -729,40 +715,118 @@ __global__ void __launch_bounds__(CC_THREADS) com_cells_kernel(ComArgs A) {
         }
     }
     __syncthreads();
-    for (uint32_t idx = d0 + threadIdx.x; idx < d1; idx += CC_THREADS) {
-        if (A.node_body[idx] == NB_NONE && A.node_last[idx] < Pend) {
-            const int l = min((int)A.node_level[idx], CM_LEVELS - 1);
-            const uint32_t slot = off[l] + atomicAdd(&fill[l], 1u);
-            if (slot < (uint32_t)CW) nodes[slot] = idx;
-            else atomicOr(A.err, NB_DEVERR_DEPTH);  // a consistent tree never gets here
+    for (uint32_t k = threadIdx.x; k < nf; k += blockDim.x) {
+        const uint32_t l = flev[k];
+        nodes[off[l] + atomicAdd(&fill[l], 1u)] = found[k];
+    }
+    __syncthreads();
+    for (int l = CM_LEVELS - 1; l >= 0; --l) {  // deepest level first
+        const uint32_t c = cnt[l];
+        if (c == 0) continue;  // uniform across the block
+        for (uint32_t k = threadIdx.x; k < c; k += blockDim.x)
+            sum_children(A, nodes[off[l] + k], false);
+        __syncthreads();
+    }
+    for (uint32_t k = threadIdx.x; k < nf; k += blockDim.x) cell_records(A, nodes[k]);
+}
+
+__global__ void __launch_bounds__(CC_THREADS) com_cells_kernel(ComArgs A, uint2* up,
+                                                               uint32_t* up_count) {
+    __shared__ uint32_t found[CW];  // the chunk's local cells as found
+    __shared__ uint8_t flev[CW];    // and their levels
+    __shared__ uint32_t nodes[CW];  // the same cells, grouped by level
+    __shared__ uint32_t cnt[CM_LEVELS], off[CM_LEVELS], fill[CM_LEVELS];
+    __shared__ uint32_t n_found, n_up;
+    const uint32_t P = blockIdx.x * CW;
+    if (P >= A.n) return;
+    const uint32_t Pend = min(P + (uint32_t)CW, A.n);
+    const uint32_t d0 = A.base[P], d1 = A.base[Pend];
+    for (int l = threadIdx.x; l < CM_LEVELS; l += CC_THREADS) cnt[l] = fill[l] = 0;
+    if (threadIdx.x == 0) n_found = n_up = 0;
+    __syncthreads();
+    // one scan of the chunk's node range, CC_BATCH entries per thread in flight together
+    for (uint32_t i0 = d0 + threadIdx.x; i0 < d1; i0 += CC_THREADS * CC_BATCH) {
+        uint32_t body[CC_BATCH], last[CC_BATCH];
+        uint8_t lvl[CC_BATCH];
+#pragma unroll
+        for (int k = 0; k < CC_BATCH; ++k) {
+            const uint32_t idx = i0 + k * CC_THREADS;
+            body[k] = idx < d1 ? A.node_body[idx] : 0u;
+            last[k] = idx < d1 ? A.node_last[idx] : 0u;
+            lvl[k] = idx < d1 ? A.node_level[idx] : 0;
+        }
+#pragma unroll
+        for (int k = 0; k < CC_BATCH; ++k) {
+            const uint32_t idx = i0 + k * CC_THREADS;
+            if (idx >= d1 || body[k] != NB_NONE) continue;  // past the range, or a leaf
+            const int l = min((int)lvl[k], CM_LEVELS - 1);
+            if (last[k] >= Pend) {  // reaches past the chunk: for the next tier
+                const uint32_t g = atomicAdd(&n_up, 1u);
+                if (g < (uint32_t)CM_LEVELS)
+                    up[(size_t)blockIdx.x * CM_LEVELS + g] = make_uint2(idx, (uint32_t)l);
+                else
+                    atomicOr(A.err, NB_DEVERR_DEPTH);  // more than one per level: inconsistent
+                continue;
+            }
+            atomicAdd(&cnt[l], 1u);
+            const uint32_t slot = atomicAdd(&n_found, 1u);
+            if (slot < (uint32_t)CW) {
+                found[slot] = idx;
+                flev[slot] = (uint8_t)l;
+            } else {
+                atomicOr(A.err, NB_DEVERR_DEPTH);  // a consistent tree never gets here
+            }
         }
     }
     __syncthreads();
-    uint32_t total = 0;
-    for (int l = CM_LEVELS - 1; l >= 0; --l) {
-        const uint32_t c = cnt[l];
-        if (c == 0) continue;  // uniform across the block
-        total += c;
-        for (uint32_t k = threadIdx.x; k < c && off[l] + k < (uint32_t)CW; k += CC_THREADS) {
-            const uint32_t idx = nodes[off[l] + k];
-            sum_children(A, idx, false);
-            const uint32_t par = A.node_parent[idx];
-            if (par != NB_NONE && !(par >= d0 && A.node_last[par] < Pend)) {
-                // the parent reaches past the chunk: arrive after the level loop (this thread
-                // wrote the sums, so its release covers them)
-                const uint32_t slot = atomicAdd(&n_roots, 1u);
-                if (slot < (uint32_t)CC_ROOTS) roots[slot] = make_uint2(idx, threadIdx.x);
-                else arrive_and_climb(A, idx);  // no room: arrive now
-            }
+    if (threadIdx.x == 0) up_count[blockIdx.x] = min(n_up, (uint32_t)CM_LEVELS);
+    // more local cells than a chunk's bodies allow: only an inconsistent tree (error bit set);
+    // stop here, before any index beyond what the scan recorded is used
+    if (n_found > (uint32_t)CW) return;
+    sum_by_level(A, found, flev, n_found, nodes, cnt, off, fill);
+}
+
+// Tier of `span` sorted positions per block (span = CW * CM_FAN^t): the cells listed by the
+// CM_FAN lower-tier chunks of the span (in[c * CM_LEVELS + k], k < in_count[c]) that end inside
+// it are summed here; the others go to up[] for the next tier (up == nullptr: the last tier,
+// whose single block spans all bodies).
+__global__ void __launch_bounds__(CC_THREADS)
+com_tier_kernel(ComArgs A, uint32_t span, const uint2* __restrict__ in,
+                const uint32_t* __restrict__ in_count, uint32_t in_chunks, uint2* up,
+                uint32_t* up_count) {
+    __shared__ uint32_t found[CM_TIER_MAX];
+    __shared__ uint8_t flev[CM_TIER_MAX];
+    __shared__ uint32_t nodes[CM_TIER_MAX];
+    __shared__ uint32_t cnt[CM_LEVELS], off[CM_LEVELS], fill[CM_LEVELS];
+    __shared__ uint32_t n_found, n_up;
+    const uint32_t P = blockIdx.x * span;
+    if (P >= A.n) return;
+    const uint32_t Pend = (uint32_t)min((uint64_t)P + span, (uint64_t)A.n);
+    for (int l = threadIdx.x; l < CM_LEVELS; l += CC_THREADS) cnt[l] = fill[l] = 0;
+    if (threadIdx.x == 0) n_found = n_up = 0;
+    __syncthreads();
+    const uint32_t c0 = blockIdx.x * CM_FAN, c1 = min(c0 + (uint32_t)CM_FAN, in_chunks);
+    for (uint32_t e = threadIdx.x; e < (c1 - c0) * CM_LEVELS; e += CC_THREADS) {
+        const uint32_t c = c0 + e / CM_LEVELS, k = e % CM_LEVELS;
+        if (k >= in_count[c]) continue;
+        const uint2 g = in[(size_t)c * CM_LEVELS + k];
+        if (up != nullptr && A.node_last[g.x] >= Pend) {
+            const uint32_t u = atomicAdd(&n_up, 1u);
+            if (u < (uint32_t)CM_LEVELS) up[(size_t)blockIdx.x * CM_LEVELS + u] = g;
+            else atomicOr(A.err, NB_DEVERR_DEPTH);
+            continue;
         }
-        __syncthreads();
+        atomicAdd(&cnt[g.y], 1u);
+        const uint32_t slot = atomicAdd(&n_found, 1u);
+        if (slot < (uint32_t)CM_TIER_MAX) {
+            found[slot] = g.x;
+            flev[slot] = (uint8_t)g.y;
+        }
     }
-    // records of the local cells, all lanes busy
-    for (uint32_t k = threadIdx.x; k < min(total, (uint32_t)CW); k += CC_THREADS)
-        cell_records(A, nodes[k]);
-    const uint32_t nr = min(n_roots, (uint32_t)CC_ROOTS);
-    for (uint32_t k = 0; k < nr; ++k)
-        if (roots[k].y == threadIdx.x) arrive_and_climb(A, roots[k].x);
+    __syncthreads();
+    if (threadIdx.x == 0 && up_count != nullptr) up_count[blockIdx.x] = min(n_up, (uint32_t)CM_LEVELS);
+    if (n_found > (uint32_t)CM_TIER_MAX) return;  // cannot happen: <= CM_LEVELS per chunk
+    sum_by_level(A, found, flev, n_found, nodes, cnt, off, fill);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -804,8 +868,6 @@ void carve(nb_bh_tree* t, Carver& c) {
     t->node_skip = c.take<uint32_t>(cap);
     t->node_parent = c.take<uint32_t>(cap);
     t->node_body = c.take<uint32_t>(cap);
-    t->node_nchild = c.take<uint32_t>(cap);
-    t->node_arrive = c.take<uint32_t>(cap);
     t->node_count = c.take<uint32_t>(cap);
     t->node_comx = c.take<double>(cap);
     t->node_comy = c.take<double>(cap);
@@ -820,6 +882,12 @@ void carve(nb_bh_tree* t, Carver& c) {
     t->children = c.take<uint32_t>(cap * 8);
     t->sorted4 = c.take<float4>(n);
     t->sorted4lo = c.take<float4>(n);
+    // per tier, CM_LEVELS listed cells and a count per chunk (two lists, used in turn)
+    const size_t chunks = (n + CW - 1) / CW;
+    for (int k = 0; k < 2; ++k) {
+        t->tier_cells[k] = c.take<uint2>(chunks * CM_LEVELS);
+        t->tier_count[k] = c.take<uint32_t>(chunks);
+    }
 }
 
 }  // namespace
@@ -961,13 +1029,11 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     NB_TRY(nb::check_launch("count_kernel"));
     NB_TRY(nb::exclusive_scan_u32(t->cnt, t->base, n, 1, t->scan_temp, s));
     const size_t nodes_max = 2 * (size_t)n;
-    NB_CUDA_TRY(cudaMemsetAsync(t->node_nchild, 0, nodes_max * 4, s));
-    NB_CUDA_TRY(cudaMemsetAsync(t->node_arrive, 0, nodes_max * 4, s));
     NB_CUDA_TRY(cudaMemsetAsync(t->children, 0xff, nodes_max * 8 * 4, s));  // NB_NONE
     emit_kernel<<<grid, BH_THREADS, 0, s>>>(n, t->ids, t->split_level, t->split_start, t->split_end,
                                             (const unsigned long long*)t->mask, t->base,
                                             t->node_level, t->node_first, t->node_last, t->node_skip,
-                                            t->node_parent, t->node_body, t->node_nchild, t->info,
+                                            t->node_parent, t->node_body, t->info,
                                             t->key0, t->key1, t->children);
     NB_TRY(nb::check_launch("emit_kernel"));
     NB_TRY(mark(4));
@@ -990,10 +1056,9 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     A.node_last = t->node_last;
     A.node_skip = t->node_skip;
     A.err = ctx->dev_error;
+
     A.node_parent = t->node_parent;
     A.node_body = t->node_body;
-    A.node_nchild = t->node_nchild;
-    A.node_arrive = t->node_arrive;
     A.node_count = t->node_count;
     A.comx = t->node_comx;
     A.comy = t->node_comy;
@@ -1011,8 +1076,26 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     A.sorted4lo = t->sorted4lo;
     com_leaf_kernel<<<grid, BH_THREADS, 0, s>>>(A);
     NB_TRY(nb::check_launch("com_leaf_kernel"));
-    com_cells_kernel<<<nb::ceil_div(n, CW), CC_THREADS, 0, s>>>(A);
-    NB_TRY(nb::check_launch("com_cells_kernel"));
+    {
+        uint32_t chunks = (uint32_t)nb::ceil_div(n, CW);
+        com_cells_kernel<<<chunks, CC_THREADS, 0, s>>>(A, t->tier_cells[0], t->tier_count[0]);
+        NB_TRY(nb::check_launch("com_cells_kernel"));
+        uint64_t span = CW;
+        int in = 0;
+        for (int tier = 1; tier <= CM_TIERS; ++tier) {
+            span *= CM_FAN;
+            const uint32_t blocks = (uint32_t)((n + span - 1) / span);
+            const bool last = blocks == 1;
+            com_tier_kernel<<<blocks, CC_THREADS, 0, s>>>(
+                A, (uint32_t)std::min<uint64_t>(span, 0xffffffffu), t->tier_cells[in],
+                t->tier_count[in], chunks, last ? nullptr : t->tier_cells[1 - in],
+                last ? nullptr : t->tier_count[1 - in]);
+            NB_TRY(nb::check_launch("com_tier_kernel"));
+            if (last) break;
+            chunks = blocks;
+            in = 1 - in;
+        }
+    }
     NB_TRY(mark(5));
     t->built = true;
     t->built_records = t->records;

@@ -48,6 +48,8 @@ struct nb_bh_tree {
 
     double* box = nullptr;  // [0..6] AABB (min xyz, max xyz, edge), [7..9] box centre
     uint32_t* info = nullptr;  // [0] node count (copy of base[n])
+    uint2* tier_cells[2] = {};      // centre-of-mass tiers: cells passed up, (node, level)
+    uint32_t* tier_count[2] = {};   // their count per chunk
     uint32_t* work = nullptr;  // work counter of persistent traversal kernels
     cudaEvent_t phase_ev[6] = {};  // build phase boundaries (nb_bh_set_phase_timing)
     bool phase_timing = false;
@@ -65,8 +67,8 @@ struct nb_bh_tree {
 
     uint8_t* node_level = nullptr;
     uint32_t *node_first = nullptr, *node_last = nullptr, *node_skip = nullptr;
-    uint32_t *node_parent = nullptr, *node_body = nullptr, *node_nchild = nullptr;
-    uint32_t *node_arrive = nullptr, *node_count = nullptr;
+    uint32_t *node_parent = nullptr, *node_body = nullptr;
+    uint32_t* node_count = nullptr;
     double *node_comx = nullptr, *node_comy = nullptr, *node_comz = nullptr, *node_mass = nullptr;
     NodeRec64* rec64 = nullptr;
     NodeRec32* rec32 = nullptr;
