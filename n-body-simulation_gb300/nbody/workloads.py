@@ -227,7 +227,7 @@ def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epoc
                  thetas=(0.35, 0.375, 0.4, 0.425, 0.45, 0.5), log=None):
     """Learned opening policy on the 1M-body disc + Plummer mix. The network is trained on
     labels of two training systems (seeds 11, 12); its threshold tau is chosen once, on a
-    validation system (the fastest traversal within the error bounds), and then held fixed on
+    validation system (the fastest traversal within 90% of the error bounds), and then held fixed on
     held-out systems, where it is compared with the same walk under the group theta rule at
     that system's own best theta within the bounds (the strongest theta walk, chosen with the
     evaluation system's errors), with the per-body theta rule in the same FP32 arithmetic, and with
@@ -253,7 +253,9 @@ def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epoc
 
     d, t, ref = system(validation_seed)
     val_rows = learned.sweep(ctx, t, d["G"], targets, ref, params, taus=taus, thetas=())
-    chosen = learned.best_within(val_rows, "learned")
+    # a 10% margin below the bounds on the validation system, so that the threshold is not tuned
+    # to the edge of the bounds of one system
+    chosen = learned.best_within(val_rows, "learned", median_max=0.9e-4, p99_max=0.9e-3)
     out = {
         "workload": f"{n}-body 50/50 heliocentric disc + Plummer sphere (1e-3 Msun, a = 0.05 AU, "
                     f"5 AU from the central body); FP32 forces, FP64 leapfrog, dt = 1 h",

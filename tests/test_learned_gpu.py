@@ -152,8 +152,8 @@ def test_trained_policy_gain_over_theta_walk(ctx):
 
 def test_trained_policy_holds_on_held_out_seeds(ctx):
     """The gain holds on systems the threshold was not tuned on: tau is chosen once on a
-    validation mix (the cheapest setting within 1e-4 median / 1e-3 p99 relative force error
-    against FP64 naive sums), then on three held-out mixes the learned policy at that fixed tau
+    validation mix (the cheapest setting within 80% of the 1e-4 median / 1e-3 p99 relative force
+    error bounds against FP64 naive sums), then on three held-out mixes the learned policy at that fixed tau
     stays within the bounds and needs at most 0.8x the body-cell interactions of the same walk
     with the group theta rule at each system's own cheapest theta within the bounds."""
     from nbody import generators, learned
@@ -169,7 +169,10 @@ def test_trained_policy_holds_on_held_out_seeds(ctx):
         return learned.sweep(ctx, t, d["G"], targets, ref, params, taus=taus, thetas=thetas)
 
     val = rows_for(40, (-5.0, -4.75, -4.5, -4.25, -4.0, -3.75), ())
-    chosen = learned.best_within(val, "learned", key="interactions")
+    # a 20% margin below the bounds on the validation system: the held-out systems must then
+    # stay within the bounds themselves
+    chosen = learned.best_within(val, "learned", median_max=0.8e-4, p99_max=0.8e-3,
+                                 key="interactions")
     assert chosen is not None, val
     for seed in (41, 42, 43):
         rows = rows_for(seed, (chosen["param"],), (0.25, 0.3, 0.35, 0.4, 0.45, 0.5))
