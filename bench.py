@@ -36,10 +36,18 @@ THETA = 0.5
 DT = 1.0 / 24
 EPS2 = 1e-22
 SEED = 1
-# kernels of ours launched per step: kick_drift 1, build 21 (aabb 1, keys 1, radix 10 (one
-# histogram of all digits, their offsets, 8 look-back passes), runs 1, splits 1, count 1, scan 3,
-# emit 1, centre of mass 1, records 1), traversal 1, kick 1
-LAUNCHES_PER_STEP = 24
+def launches_per_step(n: int) -> int:
+    """Kernels of ours launched per step: kick_drift 1, build (aabb 1, keys 1, radix 10 (one
+    histogram of all digits, their offsets, 8 look-back passes), runs 1, splits 1, count 1, scan 3,
+    emit 1, centre of mass: leaves 1, chunks of 4,096 bodies 1, one tier per factor of 64 above
+    the chunk until one block spans all bodies), traversal 1, kick 1."""
+    tiers, span = 0, 4096
+    while True:
+        tiers += 1
+        span *= 64
+        if span >= n:
+            break
+    return 3 + 21 + tiers
 # algorithmic FLOP of the traversal (Nyland's 20 per pair interaction for an accepted cell; an
 # opened cell costs its distance test: 3 sub, 3 mul, 2 add, 1 rsqrt, 1 mul = 10)
 FLOP_ACCEPTED, FLOP_OPENED = 20, 10
@@ -407,7 +415,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "steps/s",
                     "h2d_bytes_per_step": 8 * n * len(h2d_arrays),
                     "d2h_bytes_per_step": 8 * n * 9},
-            "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+            "gpu_launches": launches_per_step(n) * args.steps,
             "roofline": {"kernel": TRAVERSAL_KERNEL + " (traversal)", "bound": "fp64",
                          "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
                          "unit": "TFLOP/s", "frac": achieved / fp64_peak,
