@@ -6,7 +6,8 @@
 //  2. keys: per body the octant digit of every level from the reference's FP64 recurrence
 //     (mid = min + edge/2, strict compares, z below the midpoint selects bit 0; child min corner =
 //     parent min + child edge), mapped to the visit rank so that ascending keys are the
-//     reference's DFS pop order.
+//     reference's DFS pop order; read off a 52-bit fixed-point position wherever the body is
+//     provably far enough from every midpoint for the recurrence's rounding not to matter.
 //  3. stable LSD radix sort of (key, body id).
 //  4. bodies whose first 21 digits collide get their next 21 digits and are re-sorted in place.
 //  5. splits: adjacent sorted bodies share a prefix of L digits; the split belongs to the cell at
@@ -38,11 +39,6 @@ constexpr uint32_t RUN_LIMIT = 1u << 14;  // longest run of equal first key word
 __device__ __forceinline__ uint64_t ordered_bits(double v) {
     const uint64_t u = (uint64_t)__double_as_longlong(v);
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
-}
-
-// Inverse of ordered_bits.
-__device__ __forceinline__ double from_ordered(uint64_t o) {
-    return __longlong_as_double((long long)((o >> 63) ? (o & ~0x8000000000000000ull) : ~o));
 }
 
 // The edge halvings of the recurrence: exponent decrements while they stay exact (the normal,
@@ -105,70 +101,6 @@ __device__ uint64_t key_word(const double* __restrict__ box, double px, double p
                       box[0], box[1], box[2], 0, first, first + NB_KEY_LEVELS, 0);
 }
 
-// Levels resolved through the per-block midpoint table of keys_kernel.
-constexpr int KT_LEVELS = 10;
-constexpr int KT_ENTRIES = (1 << KT_LEVELS) - 1;
-
-// First key word of every body. The top KT_LEVELS levels of each axis have at most 2^L distinct
-// cells per level, so each block first evaluates the reference's FP64 midpoints of those cells
-// once (mids[axis][2^L - 1 + prefix], prefix = the path's upper/lower bits of levels < L, with the
-// same recurrence and halvings) and the bodies then walk those levels with integer compares
-// against the table; the FP64 recurrence resumes at level KT_LEVELS from the table's mins. The
-// digits are those of key_word, bit for bit.
-__global__ void __launch_bounds__(BH_THREADS)
-keys_kernel(const double* __restrict__ x, const double* __restrict__ y,
-            const double* __restrict__ z, uint32_t n, double* __restrict__ box,
-            uint64_t* __restrict__ key0, uint32_t* __restrict__ ids) {
-    __shared__ uint64_t mids[3][KT_ENTRIES];
-    if (blockIdx.x == 0 && threadIdx.x < 3)  // box centre, for the node records
-        box[7 + threadIdx.x] = box[threadIdx.x] + box[6] / 2;
-    {
-        Halving h(box[6]);
-        for (int L = 0; L < KT_LEVELS; ++L) {
-            const double ce = h.next();
-            for (int t = threadIdx.x; t < (1 << L); t += blockDim.x) {
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    double mn = box[a];
-                    for (int l = 0; l < L; ++l)  // upper half at level l: min = that midpoint
-                        if ((t >> (L - 1 - l)) & 1)
-                            mn = from_ordered(mids[a][(1 << l) - 1 + (t >> (L - l))]);
-                    mids[a][(1 << L) - 1 + t] = ordered_bits(__dadd_rn(mn, ce));
-                }
-            }
-            __syncthreads();
-        }
-    }
-    Halving h0(box[6]);
-    for (int l = 0; l < KT_LEVELS; ++l) h0.next();  // the edge entering level KT_LEVELS
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint64_t ox = ordered_coord(x[i]), oy = ordered_coord(y[i]),
-                       oz = ordered_coord(z[i]);
-        uint64_t key = 0;
-        uint32_t tx = 0, ty = 0, tz = 0;  // paths so far (1 = upper half)
-        uint64_t ux = 0, uy = 0, uz = 0;  // last upper midpoints (ordered bits), 0 = none
-#pragma unroll
-        for (int L = 0; L < KT_LEVELS; ++L) {
-            const int base = (1 << L) - 1;
-            const uint64_t mx = mids[0][base + tx], my = mids[1][base + ty],
-                           mz = mids[2][base + tz];
-            const bool up = oy > my, rt = ox > mx, bk = oz < mz;
-            key = (key << 3) |
-                  nb_visit_of_octant((uint32_t)up * 4u + (uint32_t)rt * 2u + (uint32_t)bk);
-            tx = 2 * tx + rt;
-            ty = 2 * ty + up;
-            tz = 2 * tz + !bk;
-            if (rt) ux = mx;
-            if (up) uy = my;
-            if (!bk) uz = mz;
-        }
-        const double mnx = ux ? from_ordered(ux) : box[0], mny = uy ? from_ordered(uy) : box[1],
-                     mnz = uz ? from_ordered(uz) : box[2];
-        key0[i] = key_levels(h0, ox, oy, oz, mnx, mny, mnz, KT_LEVELS, 0, NB_KEY_LEVELS, key);
-        ids[i] = i;
-    }
-}
-
 // Quantized keys (NB_BUILD_QUANTIZED_KEYS): every coordinate as a 42-bit fraction of the box,
 // floor((v - min) * 2^42 / edge), one bit per level. Bodies fall into the cells of the
 // reference's recurrence except within FP64 rounding of a cell midpoint (there the quantized
@@ -211,6 +143,77 @@ __global__ void keys_quantized_kernel(const double* __restrict__ x, const double
     if (i < 3) box[7 + i] = box[i] + box[6] / 2;  // box centre, for the node records
     if (i >= n) return;
     key0[i] = key_word_quantized(box, x[i], y[i], z[i], 0);
+    ids[i] = i;
+}
+
+// First key word of every body, the digits of key_word bit for bit, mostly without the FP64
+// recurrence. The recurrence's midpoints differ from the dyadic grid min + (2j + 1) edge /
+// 2^(L+1) only by the rounding of its additions (the halvings are exact): after L + 1 of them by
+// at most (L + 1) 2^-53 R, R = |min| + edge bounding every midpoint, i.e. (L + 1) R / (2 edge)
+// units of edge / 2^52. A coordinate as a 52-bit fraction of the edge, U = floor((v - min) 2^52 /
+// edge), is within 1.5 units of the exact value (three roundings), so when U is more than
+// m = 10.5 R / edge + 4 units from every multiple of 2^31 (the grid boundaries of levels 0..20),
+// the digits of those levels are bits 51..31 of U. Bodies inside a margin, and boxes whose edge
+// the recurrence does not halve by exponent arithmetic, take the recurrence itself.
+struct FixedGrid {
+    double scale;  // 2^52 / edge
+    long long margin[3];
+    bool ok;
+};
+
+__device__ FixedGrid fixed_grid(const double* __restrict__ box) {
+    FixedGrid g;
+    const double e = box[6];
+    const uint64_t eb = (uint64_t)__double_as_longlong(e);
+    g.ok = (eb >> 52) > 64 && (eb >> 52) < 0x7ff;  // Halving's exponent mode: positive, normal
+    g.scale = g.ok ? 4503599627370496.0 / e : 0.0;
+    g.ok = g.ok && g.scale < 1e308;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {  // R / edge = |min| * scale / 2^52 + 1
+        const double m = 10.5 * fma(fabs(box[a]), g.scale * 0x1p-52, 1.0) * (1.0 + 0x1p-30) + 4.0;
+        g.ok = g.ok && m < 0x1p29;  // false for NaN as well
+        g.margin[a] = g.ok ? (long long)m + 1 : 0;
+    }
+    return g;
+}
+
+// Bits 51..31 of U for one axis, or -1 when U lies within the margin of a grid boundary (or the
+// coordinate is outside the box or NaN).
+__device__ __forceinline__ long long fixed_digits(double v, double mn, double scale, long long m) {
+    const double u = __dmul_rn(__dsub_rn(v, mn), scale);
+    if (!(u >= 0.0 && u <= 4503599627370496.0)) return -1;
+    const long long U = (long long)u;
+    const long long hi = (U + m) >> 31, lo = (U - m - 1) >> 31;
+    return hi == lo ? hi : -1;
+}
+
+__global__ void __launch_bounds__(BH_THREADS)
+keys_kernel(const double* __restrict__ x, const double* __restrict__ y,
+            const double* __restrict__ z, uint32_t n, double* __restrict__ box,
+            uint64_t* __restrict__ key0, uint32_t* __restrict__ ids) {
+    __shared__ FixedGrid grid_s;  // once per block: it takes an FP64 division
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 3) box[7 + i] = box[i] + box[6] / 2;  // box centre, for the node records
+    if (threadIdx.x == 0) grid_s = fixed_grid(box);
+    __syncthreads();
+    if (i >= n) return;
+    const FixedGrid g = grid_s;
+    const double px = x[i], py = y[i], pz = z[i];
+    long long hx = -1, hy = -1, hz = -1;
+    if (g.ok) {
+        hx = fixed_digits(px, box[0], g.scale, g.margin[0]);
+        hy = fixed_digits(py, box[1], g.scale, g.margin[1]);
+        hz = fixed_digits(pz, box[2], g.scale, g.margin[2]);
+    }
+    uint64_t key;
+    if ((hx | hy | hz) >= 0) {  // visit rank = 4 (y upper) + 2 (z lower) + (x lower)
+        const uint64_t m = 0x1fffffull;
+        key = (spread3((uint64_t)hy) << 2) | (spread3(~(uint64_t)hz & m) << 1) |
+              spread3(~(uint64_t)hx & m);
+    } else {
+        key = key_word(box, px, py, pz, 0);
+    }
+    key0[i] = key;
     ids[i] = i;
 }
 
@@ -1002,9 +1005,7 @@ nb_status nb_bh_build(nb_ctx* ctx, nb_bh_tree* t, const double* m, const double*
     if (quantized) {
         keys_quantized_kernel<<<grid, BH_THREADS, 0, s>>>(x, y, z, n, t->box, t->key0, t->ids);
     } else {
-        // persistent blocks: each evaluates the midpoint table once, then walks its bodies
-        keys_kernel<<<std::min(grid, 8 * ctx->sm_count), BH_THREADS, 0, s>>>(x, y, z, n, t->box,
-                                                                            t->key0, t->ids);
+        keys_kernel<<<grid, BH_THREADS, 0, s>>>(x, y, z, n, t->box, t->key0, t->ids);
     }
     NB_TRY(nb::check_launch("keys_kernel"));
     NB_TRY(mark(2));

@@ -104,13 +104,45 @@ def _clustered(n, seed):
             "z": pts[2].copy(), "G": 1.0}
 
 
+def _midpoints(n, seed):
+    """Bodies on the FP64 midpoints of the reference's key recurrence (random cells of levels
+    0..20 per axis, nudged by -2..2 ulps) mixed with uniform bodies, in a box fixed by two
+    corners: the keys kernel must take the recurrence itself for the first kind (their digits
+    depend on its rounding) and the fixed-point digits for the second, in the same warps."""
+    rng = np.random.default_rng(seed)
+    lo, hi = -1.37, 2.11
+    box = oracle.aabb(np.array([lo, hi]), np.array([lo, hi]), np.array([lo, hi]))
+    e = box["edge"]
+    cols = []
+    for a in ("x", "y", "z"):
+        mn, ce = np.full(n, box["min_" + a]), e
+        stop, v = rng.integers(0, 21, size=n), np.zeros(n)
+        for level in range(21):
+            ce = ce / 2
+            mid = mn + ce
+            v[stop == level] = mid[stop == level]
+            mn = np.where(rng.random(n) < 0.5, mid, mn)
+        cols.append(v)
+    p = np.unique(np.stack(cols, axis=1), axis=0)  # distinct cells: no near-coincident bodies
+    k = rng.integers(-2, 3, size=p.shape)
+    for s in (1, 2):
+        p[k >= s] = np.nextafter(p[k >= s], np.inf)
+        p[k <= -s] = np.nextafter(p[k <= -s], -np.inf)
+    p = np.concatenate([p, rng.uniform(lo, hi, size=(n // 3, 3))])
+    p = np.clip(rng.permutation(p), lo, hi)
+    x, y, z = (np.concatenate([[lo, hi], p[:, a]]) for a in range(3))
+    return {"m": rng.uniform(1, 2, len(x)), "x": x, "y": y, "z": z, "G": 1.0}
+
+
 @pytest.mark.parametrize("case", ["disc-2000", "plummer-5000", "disc-1", "disc-2", "plummer-3",
-                                  "clustered-4000", "shifted-3000"])
+                                  "clustered-4000", "shifted-3000", "midpoints-3000"])
 def test_tree_matches_oracle_cell_by_cell(ctx, case):
     kind, n = case.split("-")
     n = int(n)
     if kind == "clustered":
         d = _clustered(n, 3)
+    elif kind == "midpoints":
+        d = _midpoints(n, 4)
     elif kind == "shifted":
         d = bodies("plummer", n, seed=9)
         d["x"] = d["x"] + 25.0  # box must still contain the origin (reference convention)
@@ -118,7 +150,7 @@ def test_tree_matches_oracle_cell_by_cell(ctx, case):
         d = bodies(kind, n, seed=5)
     # deep clumps need more than the reference's default 16*N node slots (each level of a
     # single-child chain costs 8 slots there)
-    storage = 256 if kind == "clustered" else 16
+    storage = 256 if kind in ("clustered", "midpoints") else 16
     ot = oracle.build_subtrees(d["m"], d["x"], d["y"], d["z"], max_level=7, threads=4,
                                storage_param=storage)
     tree, _ = build(ctx, d)
