@@ -852,6 +852,10 @@ void carve(nb_bh_tree* t, Carver& c) {
     t->box = c.take<double>(16);
     t->info = c.take<uint32_t>(16);
     t->work = c.take<uint32_t>(16);
+    t->sched = c.take<uint32_t>(32);
+    t->group_cost = c.take<uint32_t>(n / 32 + 1);
+    t->group_first = c.take<uint32_t>(n / 32 + 1);
+    t->group_skip = c.take<uint32_t>(n / 1024 + 1);
     t->key0 = c.take<uint64_t>(n);
     t->key1 = c.take<uint64_t>(n);
     t->key_alt = c.take<uint64_t>(n);
@@ -934,6 +938,12 @@ nb_status nb_bh_tree_create(nb_ctx* ctx, uint32_t n_max, const nb_bh_params* par
     Carver real;
     real.base = (char*)mem;
     carve(t, real);
+    e = cudaMemset(t->sched, 0, 32 * sizeof(uint32_t));  // no group order yet
+    if (e != cudaSuccess) {
+        cudaFree(mem);
+        delete t;
+        return nb::cuda_error(e, "nb_bh_tree_create");
+    }
     // the carve order puts box first: its address is the allocation base (freed in destroy)
     *out = t;
     return NB_OK;

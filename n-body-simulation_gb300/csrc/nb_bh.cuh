@@ -51,6 +51,13 @@ struct nb_bh_tree {
     uint2* tier_cells[2] = {};      // centre-of-mass tiers: cells passed up, (node, level)
     uint32_t* tier_count[2] = {};   // their count per chunk
     uint32_t* work = nullptr;  // work counter of persistent traversal kernels
+    // group schedule of the learned traversal: each launch records a cost per group of 32
+    // bodies, from which the next launch takes its costliest groups first
+    uint32_t* group_cost = nullptr;   // per group
+    uint32_t* group_first = nullptr;  // the groups taken first (priority list)
+    uint32_t* group_skip = nullptr;   // bit per group: on the priority list
+    uint32_t* sched = nullptr;  // [0] groups the schedule is for, [1] length of the priority
+                                // list, [18..19] total cost (uint64)
     cudaEvent_t phase_ev[6] = {};  // build phase boundaries (nb_bh_set_phase_timing)
     bool phase_timing = false;
     uint32_t records = NB_REC_ALL;   // record sets the next build computes (nb_bh_set_records)

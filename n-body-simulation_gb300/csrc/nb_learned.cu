@@ -435,7 +435,13 @@ __device__ __forceinline__ void two_sum_add(float& h, float& l, float v) {
 // Interaction-list positions are relative to the group's first body and built from two-float
 // (FP32 value + FP32 residual) coordinates, so nearby pairs keep their full FP32 precision. With
 // params == nullptr the network's cells use the group theta rule instead (same walk, no network).
-template <bool COUNTED>
+// Groups are taken in tree order; when sched[0] equals the group count, the sched[1] groups of
+// `first` (the costliest of the previous launch, flagged in the bit mask `skip`) are taken before
+// all others and skipped in the tree-order pass. Each group is walked once either way, so the
+// results do not depend on the schedule. Each group's cost (2 per cell visited + 1 per list entry)
+// goes to cost[] for the next launch's schedule. NET = false is the theta-rule walk (params ==
+// nullptr), compiled without the network.
+template <bool COUNTED, bool NET>
 __global__ void __launch_bounds__(LT_THREADS, 4)
 bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__ aux,
                   const uint32_t* __restrict__ children, const float4* __restrict__ sorted4,
@@ -444,7 +450,10 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
                   float theta2, uint32_t count_cap, float eps2, const uint32_t* __restrict__ ids,
                   double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az,
                   unsigned long long* __restrict__ counters, uint32_t* __restrict__ err_word,
-                  uint32_t* __restrict__ next_group, int cap, const double* __restrict__ box) {
+                  uint32_t* __restrict__ next_group, int cap, const double* __restrict__ box,
+                  const uint32_t* __restrict__ first, const uint32_t* __restrict__ skip,
+                  const uint32_t* __restrict__ sched, uint32_t* __restrict__ cost,
+                  unsigned long long* __restrict__ cost_total) {
     // cap <= LT_CAP: the stack entries a walk may use (LT_CAP except in the failure-path tests)
     __shared__ uint32_t stack[LT_WARPS][LT_CAP];
     __shared__ __align__(16) __nv_bfloat16 feat[LT_WARPS][LT_BATCH][16];
@@ -454,18 +463,34 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
     __shared__ __align__(16) uint32_t wfrag[32 * MF_WS];
     __shared__ __align__(16) float bfrag[32 * MF_BS];
     __shared__ BoxScale bs;  // in shared memory: no registers held through the walk
+    __shared__ uint32_t n_first;  // groups of the priority list (0: tree order only)
+    __shared__ uint32_t wcost[LT_WARPS];  // cost of each warp's current group (no register)
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
-    if (threadIdx.x == 0) bs = BoxScale(box[6]);
-    if (params != nullptr && wi == 0)
-        load_frags(params, lane, wfrag + lane * MF_WS, bfrag + lane * MF_BS, 1);
-    __syncthreads();  // before any warp leaves
     const uint32_t n_groups = (n + 31) / 32;
+    if (threadIdx.x == 0) {
+        bs = BoxScale(box[6]);
+        n_first = sched[0] == n_groups ? min(sched[1], n_groups) : 0u;
+    }
+    if (NET && wi == 0) load_frags(params, lane, wfrag + lane * MF_WS, bfrag + lane * MF_BS, 1);
+    __syncthreads();  // before any warp leaves
     unsigned long long t_acc = 0, t_mlp = 0, t_cells = 0, t_steps = 0;
+    bool listed = n_first > 0;  // lane 0: still taking groups from the priority list
     // persistent warps: each takes the next group until none are left (no warp idles while its
     // block's other warps finish long walks)
     for (;;) {
         uint32_t gw = 0;
-        if (lane == 0) gw = atomicAdd(next_group, 1u);
+        if (lane == 0) {
+            if (listed) {
+                const uint32_t k = atomicAdd(next_group + 2, 1u);
+                if (k < n_first) gw = first[k];
+                else listed = false;
+            }
+            if (!listed) {
+                do {
+                    gw = atomicAdd(next_group, 1u);
+                } while (n_first > 0 && gw < n_groups && ((skip[gw >> 5] >> (gw & 31)) & 1u));
+            }
+        }
         gw = __shfl_sync(0xffffffffu, gw, 0);
         if (gw >= n_groups) break;
         const uint32_t p = gw * 32 + lane;
@@ -491,7 +516,7 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
         reinterpret_cast<float*>(gpx[wi])[lane] = valid ? ph.x : inf;
         reinterpret_cast<float*>(gpy[wi])[lane] = valid ? ph.y : inf;
         reinterpret_cast<float*>(gpz[wi])[lane] = valid ? ph.z : inf;
-        const bool use_net = params != nullptr;
+        constexpr bool use_net = NET;
         const MlpFragsSmem F{wfrag + lane * MF_WS, bfrag + lane * MF_BS};
         uint32_t* st = stack[wi];
         __nv_bfloat16* fm = &feat[wi][0][0];
@@ -501,6 +526,7 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
         float hx = 0, hy = 0, hz = 0, lx = 0, ly = 0, lz = 0;
         int list_n = 0;
         uint32_t n_acc = 0, n_mlp = 0, n_cells = 0, n_steps = 0;  // COUNTED only
+        if (lane == 0) wcost[wi] = 0;
         NodeRec32 r{};
         NodeAux xa{};
         uint4 c0, c1;
@@ -621,6 +647,7 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
             }
             const uint32_t step_total = __shfl_sync(0xffffffffu, pos, 31);
             pos -= slots;
+            if (lane == 0) wcost[wi] += 2u * (uint32_t)B + step_total;
             B = pop_and_load();  // next step's cells are in flight during the list work below
             if (list_n + (int)step_total > LT_LIST) {  // make room: sum the list so far
                 float fx, fy, fz;
@@ -652,6 +679,10 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
             ay[me] = ((double)hy + (double)ly) + (double)fy;
             az[me] = ((double)hz + (double)lz) + (double)fz;
         }
+        if (lane == 0) {
+            cost[gw] = wcost[wi];
+            atomicAdd(cost_total, (unsigned long long)wcost[wi]);
+        }
         const unsigned valid_lanes = __popc(__ballot_sync(0xffffffffu, valid));
         if (COUNTED) {
             t_acc += n_acc * (unsigned long long)valid_lanes;
@@ -667,6 +698,31 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
         atomicAdd(&counters[2], t_cells);
         atomicAdd(&counters[3], t_steps);
     }
+}
+
+// Schedule of the next learned traversal from this one's group costs: the groups costing at least
+// twice the mean go to the priority list (taken first, so that the long walks do not end the
+// launch alone) and are flagged in the skip mask; all others keep tree order, which keeps the walks
+// of neighbouring groups together in the caches.
+__global__ void sched_kernel(const uint32_t* __restrict__ cost, uint32_t n_groups,
+                             uint32_t* __restrict__ sched, uint32_t* __restrict__ first,
+                             uint32_t* __restrict__ skip) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long total = *reinterpret_cast<const unsigned long long*>(sched + 18);
+    // cost >= 2 * total / n_groups, in integers
+    const bool costly = g < n_groups && total > 0 &&
+                        (unsigned long long)cost[g] * n_groups >= 2ull * total;
+    const unsigned m = __ballot_sync(0xffffffffu, costly);
+    if (lane == 0 && g < n_groups) skip[g >> 5] = m;
+    if (m) {
+        const int leader = __ffs(m) - 1;
+        uint32_t at = 0;
+        if (lane == leader) at = atomicAdd(&sched[1], (uint32_t)__popc(m));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (costly) first[at + __popc(m & ((1u << lane) - 1u))] = g;
+    }
+    if (g == 0) sched[0] = n_groups;  // read by the next traversal, after this kernel
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1072,8 +1128,8 @@ namespace nb {
 nb_status learned_per_sm(int* out) {
     static int per_sm = 0;
     if (per_sm == 0) {
-        NB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bh_learned_kernel<false>,
-                                                                  LT_THREADS, 0));
+        NB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, bh_learned_kernel<false, true>, LT_THREADS, 0));
         if (per_sm < 1) per_sm = 1;
     }
     *out = per_sm;
@@ -1090,16 +1146,27 @@ nb_status launch_learned(nb_ctx* ctx, const nb_bh_tree* t, const double* x, cons
     int per_sm = 0;
     NB_TRY(learned_per_sm(&per_sm));
     if (blocks > ctx->sm_count * per_sm) blocks = ctx->sm_count * per_sm;
-    NB_CUDA_TRY(cudaMemsetAsync(t->work, 0, sizeof(uint32_t), s));
-    auto kernel = counters ? bh_learned_kernel<true> : bh_learned_kernel<false>;
+    // group counters (tree order, priority list) and the cost total; the schedule the previous
+    // launch left in sched[0..1], first[] and skip[] stays for this one
+    NB_CUDA_TRY(cudaMemsetAsync(t->work, 0, 3 * sizeof(uint32_t), s));
+    NB_CUDA_TRY(cudaMemsetAsync(t->sched + 18, 0, sizeof(unsigned long long), s));
+    const bool net = t->policy != nullptr;
+    auto kernel = counters ? (net ? bh_learned_kernel<true, true> : bh_learned_kernel<true, false>)
+                           : (net ? bh_learned_kernel<false, true> : bh_learned_kernel<false, false>);
     kernel<<<blocks, LT_THREADS, 0, s>>>(
         t->rec32, t->aux, t->children, t->sorted4, t->sorted4lo, t->n, t->policy,
         t->policy_log_tau * 0.2f,
         (t->policy_flags & NB_POLICY_BOUND_ACCEPT) ? exp10f(t->policy_log_tau) : 0.f,
         t->policy_theta * t->policy_theta, t->policy_count_cap,
         (float)eps2, t->ids, ax, ay, az, counters, ctx->dev_error, t->work,
-        ctx->learned_stack_cap ? (int)ctx->learned_stack_cap : LT_CAP, t->box);
-    return check_launch("bh_learned_kernel");
+        ctx->learned_stack_cap ? (int)ctx->learned_stack_cap : LT_CAP, t->box, t->group_first,
+        t->group_skip, t->sched, t->group_cost,
+        reinterpret_cast<unsigned long long*>(t->sched + 18));
+    NB_TRY(check_launch("bh_learned_kernel"));
+    NB_CUDA_TRY(cudaMemsetAsync(t->sched + 1, 0, sizeof(uint32_t), s));
+    sched_kernel<<<ceil_div((int)warps, 256), 256, 0, s>>>(t->group_cost, warps, t->sched,
+                                                           t->group_first, t->group_skip);
+    return check_launch("sched_kernel");
 }
 
 }  // namespace nb

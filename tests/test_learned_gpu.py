@@ -185,3 +185,51 @@ def test_trained_policy_holds_on_held_out_seeds(ctx):
               f"{bt['ms']:.3f} ms")
         assert lr["median"] <= 1e-4 and lr["p99"] <= 1e-3, lr
         assert lr["interactions"] <= 0.8 * bt["interactions"], (lr, bt)
+
+
+@pytest.mark.parametrize("n", [65536, 4000])
+def test_group_order_does_not_change_the_result(ctx, n):
+    """Each learned traversal records a cost per group, and the next one walks the groups
+    costliest first: the accelerations stay bit-identical to the first call's (tree order), for
+    the network and for the theta rule on the same walk, and after a rebuild with fewer bodies (a
+    stale order is not used)."""
+    import torch
+    from nbody import generators, learned
+    from nbody.lib import BHTree, BUILD_QUANTIZED_KEYS, REC_LEARNED
+    rng = np.random.default_rng(5)
+    p = torch.as_tensor((rng.normal(size=omlp.COUNT) * 0.2).astype(np.float32), device="cuda")
+    d = generators.disc_plummer_mix(n, seed=44)
+    t = learned.device_system(d)
+    tree = BHTree(ctx, n, theta=0.5)
+    tree.set_records(REC_LEARNED | BUILD_QUANTIZED_KEYS)
+    tree.build(t["m"], t["x"], t["y"], t["z"], d["G"])
+    prev = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    tree.accel(t["x"], t["y"], t["z"], *prev, d["G"], learned.EPS2, "group", "f32c")
+
+    def run():
+        acc = [v.clone() for v in prev]
+        tree.accel(t["x"], t["y"], t["z"], *acc, d["G"], learned.EPS2, "learned", "f32c")
+        ctx.sync()
+        return [v.cpu().numpy() for v in acc]
+
+    for policy in ((p, -4.0, 0.3, learned.NO_CAP), (None, 0.0, 0.4, learned.NO_CAP)):
+        tree.set_policy(*policy)
+        first = run()
+        for _ in range(2):
+            again = run()
+            for a, b in zip(first, again):
+                np.testing.assert_array_equal(a, b)
+    # fewer bodies in the same tree: the order built for the larger system must not be used
+    m = n // 2 + 17
+    tree.build(t["m"][:m], t["x"][:m], t["y"][:m], t["z"][:m], d["G"])
+    small = [v[:m].clone() for v in prev]
+    res = []
+    for _ in range(2):
+        acc = [v.clone() for v in small]
+        tree.accel(t["x"][:m], t["y"][:m], t["z"][:m], *acc, d["G"], learned.EPS2, "learned", "f32c")
+        ctx.sync()
+        res.append([v.cpu().numpy() for v in acc])
+        assert all(np.all(np.isfinite(v)) for v in res[-1])
+    for a, b in zip(*res):
+        np.testing.assert_array_equal(a, b)
+    tree.close()
