@@ -460,6 +460,8 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
     // the group's positions as packed pairs (bodies 2j, 2j+1) per axis, for the gap loop
     __shared__ nb_f2 gpx[LT_WARPS][16], gpy[LT_WARPS][16], gpz[LT_WARPS][16];
     __shared__ float4 ilist[LT_WARPS][LT_LIST];
+    // per step: the lane whose cell fills each new list slot (0xff: a monopole, written by its lane)
+    __shared__ uint8_t slot_lane[LT_WARPS][LT_BATCH * LT_DIRECT];
     __shared__ __align__(16) uint32_t wfrag[32 * MF_WS];
     __shared__ __align__(16) float bfrag[32 * MF_BS];
     __shared__ BoxScale bs;  // in shared memory: no registers held through the walk
@@ -660,12 +662,29 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
                 list_n = 0;
                 __syncwarp();
             }
-            float4* L = ilist[wi] + list_n + pos;
-            if (mono) L[0] = mono_e;
-            for (uint32_t j = 0; j < d_count; ++j) {
-                const float4 h = sorted4[d_first + j], l = sorted4lo[d_first + j];
-                L[j] = make_float4((h.x - ghx) + (l.x - glx), (h.y - ghy) + (l.y - gly),
-                                   (h.z - ghz) + (l.z - glz), h.w);
+            // the step's entries: monopoles from their lanes' registers; the bodies of body leaves
+            // and small opened cells loaded by the whole warp, one slot per lane and pass, so the
+            // loads of all cells are in flight together
+            float4* L = ilist[wi] + list_n;
+            uint8_t* owner = slot_lane[wi];
+            if (mono) {
+                L[pos] = mono_e;
+                owner[pos] = 0xffu;
+            }
+            for (uint32_t j = 0; j < d_count; ++j) owner[pos + j] = (uint8_t)lane;
+            __syncwarp();
+            for (uint32_t e0 = 0; e0 < step_total; e0 += 32) {  // warp-uniform trip count
+                const uint32_t e = e0 + lane;
+                const uint32_t o = e < step_total ? owner[e] : 0xffu;
+                const int src = o == 0xffu ? 0 : (int)o;
+                const uint32_t f = __shfl_sync(0xffffffffu, d_first, src);
+                const uint32_t p0 = __shfl_sync(0xffffffffu, pos, src);
+                if (o != 0xffu) {
+                    const uint32_t b = f + (e - p0);
+                    const float4 h = sorted4[b], l = sorted4lo[b];
+                    L[e] = make_float4((h.x - ghx) + (l.x - glx), (h.y - ghy) + (l.y - gly),
+                                       (h.z - ghz) + (l.z - glz), h.w);
+                }
             }
             list_n += (int)step_total;
             if (COUNTED) n_acc += step_total;
