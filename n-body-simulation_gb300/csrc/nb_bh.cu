@@ -538,9 +538,9 @@ __device__ void write_records(const ComArgs& A, uint32_t idx, double cx, double 
 // Sums of internal node `idx` from its children (the reference's octant order 0..7, FP64 adds:
 // bit-identical to BarnesHutOctree.cpp:304-311), its records, and its child list rewritten as the
 // compacted visit-order list the learned traversal reads (emit_kernel wrote it by visit rank).
-__device__ void sum_children(const ComArgs& A, uint32_t idx, bool records) {
+// c0, c1: the cell's child list as emit_kernel wrote it (loaded by the caller, possibly earlier).
+__device__ void sum_children(const ComArgs& A, uint32_t idx, bool records, uint4 c0, uint4 c1) {
     uint4* cl = reinterpret_cast<uint4*>(A.children + (size_t)idx * 8);
-    const uint4 c0 = __ldcg(cl), c1 = __ldcg(cl + 1);
     const uint32_t vs[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
     const bool learned = (A.records & NB_REC_LEARNED) != 0;
     // every child's sums requested before the first is used (one round trip, not eight)
@@ -723,12 +723,32 @@ __device__ void sum_by_level(const ComArgs& A, const uint32_t* found, const uint
         nodes[off[l] + atomicAdd(&fill[l], 1u)] = found[k];
     }
     __syncthreads();
-    for (int l = CM_LEVELS - 1; l >= 0; --l) {  // deepest level first
+    // deepest level first; each thread's first cell of the next level has its child list loaded
+    // before the barrier (a list only changes when its own cell is summed), so a level costs one
+    // round trip to the children's sums instead of two
+    const uint4 none4 = make_uint4(NB_NONE, NB_NONE, NB_NONE, NB_NONE);
+    auto list_of = [&](uint32_t idx, uint4& c0, uint4& c1) {
+        const uint4* cl = reinterpret_cast<const uint4*>(A.children + (size_t)idx * 8);
+        c0 = __ldcg(cl);
+        c1 = __ldcg(cl + 1);
+    };
+    int l = CM_LEVELS - 1;
+    while (l >= 0 && cnt[l] == 0) --l;  // uniform across the block
+    uint4 p0 = none4, p1 = none4;
+    if (l >= 0 && threadIdx.x < cnt[l]) list_of(nodes[off[l] + threadIdx.x], p0, p1);
+    while (l >= 0) {
         const uint32_t c = cnt[l];
-        if (c == 0) continue;  // uniform across the block
-        for (uint32_t k = threadIdx.x; k < c; k += blockDim.x)
-            sum_children(A, nodes[off[l] + k], false);
+        int next = l - 1;
+        while (next >= 0 && cnt[next] == 0) --next;
+        for (uint32_t k = threadIdx.x; k < c; k += blockDim.x) {
+            const uint32_t idx = nodes[off[l] + k];
+            uint4 c0 = p0, c1 = p1;
+            if (k != threadIdx.x) list_of(idx, c0, c1);
+            sum_children(A, idx, false, c0, c1);
+        }
+        if (next >= 0 && threadIdx.x < cnt[next]) list_of(nodes[off[next] + threadIdx.x], p0, p1);
         __syncthreads();
+        l = next;
     }
     for (uint32_t k = threadIdx.x; k < nf; k += blockDim.x) cell_records(A, nodes[k]);
 }
