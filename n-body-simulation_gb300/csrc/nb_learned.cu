@@ -614,41 +614,38 @@ bh_learned_kernel(const NodeRec32* __restrict__ rec, const NodeAux* __restrict__
             const bool direct = body_leaf || (live && !accept && xa.count <= LT_DIRECT);
             const bool mono = live && accept && !body_leaf;
             const bool open = live && !accept && !direct;
-            // push the children of opened cells (8-entry child lists, NB_NONE padded)
-            {
-                uint32_t nchild = 0;
-                if (open) {
-                    const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+            // push the children of opened cells (8-entry child lists, NB_NONE padded) and place the
+            // step's list entries: one warp scan of both counts (each <= 8 per lane, so the packed
+            // 16-bit halves cannot carry into each other)
+            uint32_t nchild = 0;
+            if (open) {
+                const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
     #pragma unroll
-                    for (int q = 0; q < 8; ++q) nchild += v[q] != NB_NONE;
-                }
-                uint32_t off = nchild;
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t v = __shfl_up_sync(0xffffffffu, off, o);
-                    if (lane >= o) off += v;
-                }
-                const uint32_t total = __shfl_sync(0xffffffffu, off, 31);
-                off -= nchild;
+                for (int q = 0; q < 8; ++q) nchild += v[q] != NB_NONE;
+            }
+            const uint32_t d_first = xa.first, d_count = direct ? xa.count : 0u;
+            const uint32_t slots = direct ? d_count : (mono ? 1u : 0u);
+            uint32_t scan = nchild | (slots << 16);
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, scan, o);
+                if (lane >= o) scan += v;
+            }
+            const uint32_t totals = __shfl_sync(0xffffffffu, scan, 31);
+            {
+                const uint32_t off = (scan & 0xffffu) - nchild;
                 if (nchild) {
                     const uint32_t v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
     #pragma unroll
                     for (int q = 0; q < 8; ++q)
                         if (q < (int)nchild) st[top + off + q] = v[q];
                 }
-                top += (int)total;
+                top += (int)(totals & 0xffffu);
             }
             // what the interaction list needs from this step, before the next step's loads land
             const float4 mono_e = make_float4((r.cx - ghx) - glx, (r.cy - ghy) - gly,
                                               (r.cz - ghz) - glz, r.gm);
-            const uint32_t d_first = xa.first, d_count = direct ? xa.count : 0u;
-            const uint32_t slots = direct ? d_count : (mono ? 1u : 0u);
-            uint32_t pos = slots;
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t v = __shfl_up_sync(0xffffffffu, pos, o);
-                if (lane >= o) pos += v;
-            }
-            const uint32_t step_total = __shfl_sync(0xffffffffu, pos, 31);
-            pos -= slots;
+            const uint32_t step_total = totals >> 16;
+            const uint32_t pos = (scan >> 16) - slots;
             if (lane == 0) wcost[wi] += 2u * (uint32_t)B + step_total;
             B = pop_and_load();  // next step's cells are in flight during the list work below
             if (list_n + (int)step_total > LT_LIST) {  // make room: sum the list so far
