@@ -358,7 +358,11 @@ nb_status nb_bh_set_phase_timing(nb_bh_tree* tree, int enable);
 nb_status nb_bh_build_phase_ms(nb_bh_tree* tree, float* ms5);
 
 /* Replaces BarnesHutAlgorithm::computeAccelerations (BarnesHutAlgorithm.hpp:43-46,
- * BarnesHutAlgorithm.cpp:280-401) for the bodies of the last build (same x, y, z). */
+ * BarnesHutAlgorithm.cpp:280-401) for the bodies of the last build (same x, y, z). The tree holds
+ * the persistent traversals' work counters and, for NB_OPEN_LEARNED, the cost of each group of 32
+ * bodies from the last learned traversal, from which the next one takes its costliest groups first
+ * (the results do not depend on that order); calls on one tree therefore run one after another (on
+ * one stream, or ordered by events), never concurrently. */
 nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* tree, const double* x, const double* y,
                       const double* z, double* ax, double* ay, double* az, double G, double eps2,
                       nb_opening opening, nb_precision prec, nb_stream_t stream);
