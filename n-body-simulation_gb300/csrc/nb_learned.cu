@@ -169,8 +169,10 @@ __device__ __forceinline__ void mma16816(float* c, uint32_t a0, uint32_t a1, uin
 // They live in shared memory, shared by the block's warps, [lane][index] with row strides of 28
 // and 20 words, so that a layer's fragments come in 16-byte loads (6 for the weights, 5 for the
 // biases) and the 8 lanes of each load phase hit disjoint banks.
-constexpr int MF_W = 24, MF_B = 17;
+constexpr int MF_W = 24, MF_B = 17;    // weight fragments and biases per lane
 constexpr int MF_WS = 28, MF_BS = 20;  // per-lane strides (words)
+static_assert(MF_WS >= MF_W && MF_BS >= MF_B && MF_WS % 4 == 0 && MF_BS % 4 == 0,
+              "a lane's fragments fit its 16-byte-aligned row");
 struct MlpFragsSmem {
     const uint32_t* ws;  // this lane's weight fragments
     const float* bs;     // this lane's biases
