@@ -40,14 +40,15 @@ def launches_per_step(n: int) -> int:
     """Kernels of ours launched per step: kick_drift 1, build (aabb 1, keys 1, radix 10 (one
     histogram of all digits, their offsets, 8 look-back passes), runs 1, splits 1, count 1, scan 3,
     emit 1, centre of mass: leaves 1, chunks of 4,096 bodies 1, one tier per factor of 64 above
-    the chunk until one block spans all bodies), traversal 1, kick 1."""
+    the chunk until one block spans all bodies), walk order from the last walk lengths 1,
+    traversal 1, kick 1."""
     tiers, span = 0, 4096
     while True:
         tiers += 1
         span *= 64
         if span >= n:
             break
-    return 3 + 21 + tiers
+    return 4 + 21 + tiers
 # algorithmic FLOP of the traversal (Nyland's 20 per pair interaction for an accepted cell; an
 # opened cell costs its distance test: 3 sub, 3 mul, 2 add, 1 rsqrt, 1 mul = 10)
 FLOP_ACCEPTED, FLOP_OPENED = 20, 10

@@ -876,6 +876,8 @@ void carve(nb_bh_tree* t, Carver& c) {
     t->group_cost = c.take<uint32_t>(n / 32 + 1);
     t->group_first = c.take<uint32_t>(n / 32 + 1);
     t->group_skip = c.take<uint32_t>(n / 1024 + 1);
+    t->walk_len = c.take<uint32_t>(n);
+    t->walk_ids = c.take<uint32_t>(n);
     t->key0 = c.take<uint64_t>(n);
     t->key1 = c.take<uint64_t>(n);
     t->key_alt = c.take<uint64_t>(n);

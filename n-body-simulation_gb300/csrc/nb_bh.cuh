@@ -58,6 +58,11 @@ struct nb_bh_tree {
     uint32_t* group_skip = nullptr;   // bit per group: on the priority list
     uint32_t* sched = nullptr;  // [0] groups the schedule is for, [1] length of the priority
                                 // list, [18..19] total cost (uint64)
+    // per-body walk lengths of the last per-body FP64 traversal (accepted cells, by body id) and
+    // the walk order the next one takes from them; walk_n = bodies they were recorded for (0: none)
+    uint32_t* walk_len = nullptr;
+    uint32_t* walk_ids = nullptr;
+    mutable uint32_t walk_n = 0;
     cudaEvent_t phase_ev[6] = {};  // build phase boundaries (nb_bh_set_phase_timing)
     bool phase_timing = false;
     uint32_t records = NB_REC_ALL;   // record sets the next build computes (nb_bh_set_records)

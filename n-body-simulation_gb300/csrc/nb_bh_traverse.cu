@@ -137,7 +137,10 @@ bh_theta_f64_kernel(const NodeRec64* __restrict__ rec, const uint32_t* __restric
 // FP32 error bound of d^2 with positions rounded relative to the box centre (|c-a|, |p-a| <=
 // E/2 per axis, u = 2^-24): |d2f - d2| <= u d^2 (2*sqrt(3) E/d + 5); the test below widens it
 // by 4x and adds the roundings of edge^2 and theta^2*d2f. Accumulation order per body is the
-// reference's DFS order, so MODE IEEE64 stays bit-identical.
+// reference's DFS order, so MODE IEEE64 stays bit-identical. Warps take groups of 32 sorted
+// positions; with `order` != nullptr the bodies of the positions come from it (the previous
+// walk's lengths regrouped within windows, regroup_kernel) instead of from ids. Each body's
+// accepted-cell count goes to walk_len[body].
 template <int MODE>
 __global__ void __launch_bounds__(TR_THREADS)
 bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __restrict__ rec64,
@@ -146,7 +149,8 @@ bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __res
                      const double* __restrict__ z, const double* __restrict__ box, uint32_t n,
                      double theta, double eps2, double G, double* __restrict__ ax,
                      double* __restrict__ ay, double* __restrict__ az,
-                     uint32_t* __restrict__ next_group) {
+                     uint32_t* __restrict__ next_group, const uint32_t* __restrict__ order,
+                     uint32_t* __restrict__ walk_len) {
     using A = Arith<MODE>;
     const uint32_t n_groups = (n + 31) / 32;
     const int lane = threadIdx.x & 31;
@@ -160,7 +164,8 @@ bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __res
         const uint32_t p = grp * 32 + lane;
         const bool valid = p < n;  // lanes past the end stay (they take part in the warp votes)
         const uint32_t nn = info[0];
-        const uint32_t me = valid ? ids[p] : NB_NONE;
+        const uint32_t me = valid ? (order != nullptr ? order[p] : ids[p]) : NB_NONE;
+        uint32_t accepted = 0;
         const double px = valid ? x[me] : 0.0, py = valid ? y[me] : 0.0, pz = valid ? z[me] : 0.0;
         const double E = box[6];
         const double ox = box[0] + E / 2, oy = box[1] + E / 2, oz = box[2] + E / 2;
@@ -209,6 +214,7 @@ bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __res
             }
             if (!__any_sync(0xffffffffu, found)) break;
             if (found) {
+                ++accepted;
                 const NodeRec64 q = rec64[k];
                 if (q.mass != 0) {
                     const double dx = A::sub(q.cx, px), dy = A::sub(q.cy, py), dz = A::sub(q.cz, pz);
@@ -221,8 +227,40 @@ bh_theta_lane_kernel(const NodeRec32* __restrict__ rec32, const NodeRec64* __res
             ax[me] = A::mul(acx, G);
             ay[me] = A::mul(acy, G);
             az[me] = A::mul(acz, G);
+            walk_len[me] = accepted;
         }
     }
+}
+
+// Walk order of the next per-body traversal: within each window of RG_WINDOW sorted positions
+// (bodies close together in the tree), the bodies by decreasing length of their last walk (ties
+// by position), so that the 32 lanes of a warp walk sequences of similar length and fewer lanes
+// sit idle while the FP64 monopoles of the others run (a warp instruction costs the FP64 pipe the
+// same however few lanes are active). Bitonic sort of (length, position) keys in shared memory.
+constexpr int RG_WINDOW = 1024;
+
+__global__ void __launch_bounds__(RG_WINDOW)
+regroup_kernel(const uint32_t* __restrict__ ids, const uint32_t* __restrict__ walk_len, uint32_t n,
+               uint32_t* __restrict__ order) {
+    __shared__ unsigned long long key[RG_WINDOW];
+    const uint32_t i = threadIdx.x, p = blockIdx.x * RG_WINDOW + i;
+    // ascending keys: longest walk first, then position; positions past n sort last
+    key[i] = p < n ? ((unsigned long long)(~walk_len[ids[p]]) << 32) | i : ~0ull;
+    __syncthreads();
+    for (uint32_t k = 2; k <= RG_WINDOW; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            const uint32_t q = i ^ j;
+            if (q > i) {
+                const unsigned long long a = key[i], b = key[q];
+                if (((i & k) == 0) == (a > b)) {
+                    key[i] = b;
+                    key[q] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (p < n) order[p] = ids[blockIdx.x * RG_WINDOW + (uint32_t)(key[i] & 0xffffffffu)];
 }
 
 // Per-body reference rule with FP64-accurate double-float monopoles (NB_DF64). The walk and the
@@ -598,10 +636,21 @@ nb_status launch_lane(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
     int grid = nb::ceil_div(t->n, TR_THREADS);
     if (grid > ctx->sm_count * ps) grid = ctx->sm_count * ps;
     NB_CUDA_TRY(cudaMemsetAsync(t->work + 1, 0, sizeof(uint32_t), s));
+    // the walk lengths of the last traversal of the same bodies order this one's groups (the
+    // results do not depend on the order: each body sums its own sequence)
+    const uint32_t* order = nullptr;
+    if (t->walk_n == t->n) {
+        regroup_kernel<<<nb::ceil_div(t->n, RG_WINDOW), RG_WINDOW, 0, s>>>(t->ids, t->walk_len,
+                                                                           t->n, t->walk_ids);
+        NB_TRY(nb::check_launch("regroup_kernel"));
+        order = t->walk_ids;
+    }
     bh_theta_lane_kernel<MODE><<<grid, TR_THREADS, 0, s>>>(
         t->rec32, t->rec64, t->info, t->ids, x, y, z, t->box, t->n, t->params.theta, eps2, G, ax,
-        ay, az, t->work + 1);
-    return nb::check_launch(MODE == IEEE64 ? "bh_theta_lane_kernel<ieee>" : "bh_theta_lane_kernel");
+        ay, az, t->work + 1, order, t->walk_len);
+    NB_TRY(nb::check_launch(MODE == IEEE64 ? "bh_theta_lane_kernel<ieee>" : "bh_theta_lane_kernel"));
+    t->walk_n = t->n;
+    return NB_OK;
 }
 
 }  // namespace

@@ -165,6 +165,41 @@ def test_tree_matches_oracle_cell_by_cell(ctx, case):
         assert st["max_depth"] > 21  # exercised the second key word
 
 
+@pytest.mark.parametrize("precision", ["f64_ieee", "f64"])
+def test_walk_order_from_the_last_walk_lengths_is_bit_identical(ctx, precision):
+    """The per-body FP64 traversal groups its bodies by the walk lengths of the tree's previous
+    traversal (within windows of 1,024 sorted positions): a repeated call, and a call after the
+    bodies moved and the tree was rebuilt, equal a fresh tree's first call (tree order) bit for
+    bit, and the first call matches the oracle's traversal."""
+    import torch
+    from nbody.lib import BHTree
+    d = bodies("disc", 5000, seed=8)
+    tree, dd = build(ctx, d, theta=0.5)
+    a1 = accel(ctx, tree, dd, d["G"], 1e-22, "theta", precision)
+    a2 = accel(ctx, tree, dd, d["G"], 1e-22, "theta", precision)
+    for u, v in zip(a1, a2):
+        np.testing.assert_array_equal(u, v)
+    if precision == "f64_ieee":
+        ot = oracle.build_subtrees(d["m"], d["x"], d["y"], d["z"], max_level=7, threads=4)
+        ref = oracle.bh_accel(ot, d["x"], d["y"], d["z"], d["G"], 1e-22, 0.5, threads=4)
+        for u, v in zip(a1, ref):
+            np.testing.assert_array_equal(u, v)
+    # moved bodies, same tree (history from the previous positions) vs a fresh tree
+    rng = np.random.default_rng(3)
+    for k in ("x", "y", "z"):
+        d[k] = d[k] * (1 + 1e-3 * rng.standard_normal(len(d[k])))
+    dd2 = {k: dev(d[k]) for k in ("m", "x", "y", "z")}
+    tree.build(dd2["m"], dd2["x"], dd2["y"], dd2["z"], d["G"])
+    ctx.sync()
+    b1 = accel(ctx, tree, dd2, d["G"], 1e-22, "theta", precision)
+    fresh, _ = build(ctx, d, theta=0.5)
+    b2 = accel(ctx, fresh, dd2, d["G"], 1e-22, "theta", precision)
+    for u, v in zip(b1, b2):
+        np.testing.assert_array_equal(u, v)
+    tree.close()
+    fresh.close()
+
+
 def test_coincident_bodies_report_depth_overflow(ctx):
     from nbody.lib import NBodyError, BHTree
     d = bodies("plummer", 100, seed=1)
