@@ -281,12 +281,14 @@ bh_theta_df_kernel(const NodeRec32* __restrict__ rec32, const float4* __restrict
                    const double* __restrict__ y, const double* __restrict__ z,
                    const double* __restrict__ box, uint32_t n, double theta, double eps2,
                    double gscale, double* __restrict__ ax, double* __restrict__ ay,
-                   double* __restrict__ az) {
+                   double* __restrict__ az, const uint32_t* __restrict__ order,
+                   uint32_t* __restrict__ walk_len) {
     using A = Arith<FAST64>;
     const uint32_t p = blockIdx.x * TR_THREADS + threadIdx.x;
     if (p >= n) return;
     const uint32_t nn = info[0];
-    const uint32_t me = ids[p];
+    const uint32_t me = order != nullptr ? order[p] : ids[p];  // as bh_theta_lane_kernel
+    uint32_t accepted = 0;
     const double px = x[me], py = y[me], pz = z[me];
     const double E = box[6];
     const double ox = box[0] + E / 2, oy = box[1] + E / 2, oz = box[2] + E / 2;
@@ -326,6 +328,7 @@ bh_theta_df_kernel(const NodeRec32* __restrict__ rec32, const float4* __restrict
             }
         }
         if (accept) {
+            ++accepted;
             const float4 lo = rec32lo[k];
             if (r.gm != 0.f || lo.w != 0.f) {
                 const float4 lo2 = rec32lo2[k];
@@ -369,6 +372,7 @@ bh_theta_df_kernel(const NodeRec32* __restrict__ rec32, const float4* __restrict
             k = k + 1;
         }
     }
+    walk_len[me] = accepted;
     ax[me] = ((double)ahx + (double)alx) * gscale;
     ay[me] = ((double)ahy + (double)aly) * gscale;
     az[me] = ((double)ahz + (double)alz) * gscale;
@@ -619,6 +623,19 @@ nb_status lane_per_sm(int* out) {
     return NB_OK;
 }
 
+// The walk lengths of the last per-body traversal of the same bodies order this one's groups
+// (*order = the regrouped bodies), else tree order (*order = nullptr). The results do not depend
+// on the order: each body sums its own sequence.
+nb_status walk_order(const nb_bh_tree* t, cudaStream_t s, const uint32_t** order) {
+    *order = nullptr;
+    if (t->walk_n != t->n) return NB_OK;
+    regroup_kernel<<<nb::ceil_div(t->n, RG_WINDOW), RG_WINDOW, 0, s>>>(t->ids, t->walk_len, t->n,
+                                                                       t->walk_ids);
+    NB_TRY(nb::check_launch("regroup_kernel"));
+    *order = t->walk_ids;
+    return NB_OK;
+}
+
 // Persistent launch of bh_theta_lane_kernel: resident blocks only, groups from work[1], at most
 // LANE_BLOCKS_PER_SM blocks per SM. With all 40 resident warps of an SM contending for its FP64
 // pipe, the warps that lose the arbitration keep their first group for the whole launch and
@@ -636,15 +653,8 @@ nb_status launch_lane(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
     int grid = nb::ceil_div(t->n, TR_THREADS);
     if (grid > ctx->sm_count * ps) grid = ctx->sm_count * ps;
     NB_CUDA_TRY(cudaMemsetAsync(t->work + 1, 0, sizeof(uint32_t), s));
-    // the walk lengths of the last traversal of the same bodies order this one's groups (the
-    // results do not depend on the order: each body sums its own sequence)
     const uint32_t* order = nullptr;
-    if (t->walk_n == t->n) {
-        regroup_kernel<<<nb::ceil_div(t->n, RG_WINDOW), RG_WINDOW, 0, s>>>(t->ids, t->walk_len,
-                                                                           t->n, t->walk_ids);
-        NB_TRY(nb::check_launch("regroup_kernel"));
-        order = t->walk_ids;
-    }
+    NB_TRY(walk_order(t, s, &order));
     bh_theta_lane_kernel<MODE><<<grid, TR_THREADS, 0, s>>>(
         t->rec32, t->rec64, t->info, t->ids, x, y, z, t->box, t->n, t->params.theta, eps2, G, ax,
         ay, az, t->work + 1, order, t->walk_len);
@@ -704,10 +714,16 @@ nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* t, const double* x, const d
                 if (t->G == 0)
                     return nb::set_error(NB_ERR_INVALID_ARG,
                                          "nb_bh_accel: NB_DF64 needs a build with G != 0");
+            {
+                const uint32_t* order = nullptr;
+                NB_TRY(walk_order(t, s, &order));
                 bh_theta_df_kernel<<<grid, TR_THREADS, 0, s>>>(
                     t->rec32, t->rec32lo, t->rec32lo2, t->rec64, t->info, t->ids, x, y, z, t->box,
-                    n, theta, eps2, G / t->G, ax, ay, az);
-                return nb::check_launch("bh_theta_df_kernel");
+                    n, theta, eps2, G / t->G, ax, ay, az, order, t->walk_len);
+                NB_TRY(nb::check_launch("bh_theta_df_kernel"));
+                t->walk_n = t->n;
+                return NB_OK;
+            }
             case NB_F32C:
                 if (G != t->G)
                     return nb::set_error(NB_ERR_INVALID_ARG, "nb_bh_accel: G differs from the build's");
