@@ -252,10 +252,12 @@ def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epoc
         return d, t, learned.fp64_reference(ctx, t, d["G"], targets)
 
     d, t, ref = system(validation_seed)
-    val_rows = learned.sweep(ctx, t, d["G"], targets, ref, params, taus=taus, thetas=())
+    val_rows = learned.sweep(ctx, t, d["G"], targets, ref, params, taus=taus, thetas=thetas)
     # a 10% margin below the bounds on the validation system, so that the threshold is not tuned
-    # to the edge of the bounds of one system
+    # to the edge of the bounds of one system; theta chosen the same way for the symmetric
+    # comparison (the primary one takes each held-out system's own best theta, no margin)
     chosen = learned.best_within(val_rows, "learned", median_max=0.9e-4, p99_max=0.9e-3)
+    theta_val = learned.best_within(val_rows, "theta-walk", median_max=0.9e-4, p99_max=0.9e-3)
     out = {
         "workload": f"{n}-body 50/50 heliocentric disc + Plummer sphere (1e-3 Msun, a = 0.05 AU, "
                     f"5 AU from the central body); FP32 forces, FP64 leapfrog, dt = 1 h",
@@ -263,7 +265,8 @@ def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epoc
                      "epochs": epochs, "train_s": t_train, "mse_per_epoch": hist},
         "error_bounds": {"median": 1e-4, "p99": 1e-3, "bodies": len(targets),
                          "against": "FP64 naive sums (nb_naive_accel_targets)"},
-        "validation": {"seed": validation_seed, "sweep": val_rows, "chosen": chosen},
+        "validation": {"seed": validation_seed, "sweep": val_rows, "chosen": chosen,
+                       "theta_walk_chosen": theta_val},
     }
     if chosen is None:
         out["error"] = "no threshold within the bounds on the validation system"
@@ -286,6 +289,15 @@ def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epoc
                                       policy=(None, 0.0, bt["param"], learned.NO_CAP))
             rec["theta_walk_ms_per_step"] = ms_t
             rec["speedup_vs_theta_walk_matched_error"] = ms_t / ms_l
+        if theta_val:  # theta fixed on the validation system like tau
+            tv = [r for r in rows if r["kind"] == "theta-walk" and r["param"] == theta_val["param"]]
+            ms_tv = (ms_t if bt and bt["param"] == theta_val["param"] else
+                     learned.time_steps(ctx, t, G, steps, "learned", "f32c",
+                                        policy=(None, 0.0, theta_val["param"], learned.NO_CAP)))
+            rec["theta_walk_validation_choice"] = {
+                "param": theta_val["param"], "ms_per_step": ms_tv,
+                "median": tv[0]["median"] if tv else None, "p99": tv[0]["p99"] if tv else None,
+                "speedup_of_learned": ms_tv / ms_l}
         if k == 0:  # the per-body rules and the 200-step errors on the first held-out system
             tree = BHTree(ctx, n, theta=0.5)
             tree.build(t["m"], t["x"], t["y"], t["z"], G)
@@ -317,16 +329,27 @@ def learned_form(ctx: Context, n: int = 1 << 20, n_pairs: int = 10_000_000, epoc
             checkpoints = tuple(range(0, error_steps + 1, 50))
             rec["learned_error_over_steps"] = learned.error_over_steps(
                 ctx, t, G, error_steps, checkpoints, targets, "learned", "f32c", policy=policy)
+            rec["learned_within_bounds_over_run"] = all(
+                e["median"] <= 1e-4 and e["p99"] <= 1e-3 for e in rec["learned_error_over_steps"])
             if bt:
                 rec["theta_walk_error_over_steps"] = learned.error_over_steps(
                     ctx, t, G, error_steps, checkpoints, targets, "learned", "f32c",
                     policy=(None, 0.0, bt["param"], learned.NO_CAP))
+                rec["theta_walk_within_bounds_over_run"] = all(
+                    e["median"] <= 1e-4 and e["p99"] <= 1e-3
+                    for e in rec["theta_walk_error_over_steps"])
         per_seed.append(rec)
     out["log10_tau"] = tau
     out["held_out"] = per_seed
     sp = [r.get("speedup_vs_theta_walk_matched_error") for r in per_seed]
     out["speedup_vs_theta_walk_matched_error"] = {
         "per_seed": sp, "min": min(x for x in sp if x) if any(sp) else None,
-        "all_learned_within_bounds": all(r["learned_within_bounds"] for r in per_seed)}
+        "all_learned_within_bounds": all(r["learned_within_bounds"] for r in per_seed),
+        "theta": "each held-out system's own fastest theta within the bounds (no margin)"}
+    spv = [r["theta_walk_validation_choice"]["speedup_of_learned"]
+           for r in per_seed if "theta_walk_validation_choice" in r]
+    out["speedup_vs_theta_walk_validation_choice"] = {
+        "per_seed": spv, "min": min(spv) if spv else None,
+        "theta": "fixed on the validation system with the same 10% margin as tau"}
     out["learned_steps_per_s"] = 1e3 / per_seed[0]["learned_ms_per_step"]
     return out
