@@ -359,10 +359,12 @@ nb_status nb_bh_build_phase_ms(nb_bh_tree* tree, float* ms5);
 
 /* Replaces BarnesHutAlgorithm::computeAccelerations (BarnesHutAlgorithm.hpp:43-46,
  * BarnesHutAlgorithm.cpp:280-401) for the bodies of the last build (same x, y, z). The tree holds
- * the persistent traversals' work counters and, for NB_OPEN_LEARNED, the cost of each group of 32
- * bodies from the last learned traversal, from which the next one takes its costliest groups first
- * (the results do not depend on that order); calls on one tree therefore run one after another (on
- * one stream, or ordered by events), never concurrently. */
+ * the persistent traversals' work counters, each body's walk length from the last per-body
+ * traversal (NB_OPEN_THETA with NB_F64, NB_F64_IEEE or NB_DF64), from which the next one of the
+ * same bodies groups its bodies, and for NB_OPEN_LEARNED the cost of each group of 32 bodies from
+ * the last learned traversal, from which the next one takes its costliest groups first; the
+ * results do not depend on either order. Calls on one tree therefore run one after another (on one
+ * stream, or ordered by events), never concurrently. */
 nb_status nb_bh_accel(nb_ctx* ctx, const nb_bh_tree* tree, const double* x, const double* y,
                       const double* z, double* ax, double* ay, double* az, double G, double eps2,
                       nb_opening opening, nb_precision prec, nb_stream_t stream);
