@@ -779,6 +779,31 @@ def build_case(n: int = 1 << 20, mask: str = "fp64"):
     tree.close()
 
 
+def leapfrog_case(n: int = 1 << 20, n_energy: int = 16384):
+    """The leapfrog kernels on the seeded 1,048,576-body disc (HBM-bound: 120 and 72 bytes per
+    body) and the energy (an O(N^2) FP64 pair sum, like the naive kernel) on its first 16,384
+    bodies: three calls each."""
+    import torch
+
+    from nbody import generators, learned
+    from nbody.lib import Context
+    ctx = Context(0)
+    d = generators.heliocentric_disc(n, 1)
+    t = learned.device_system(d)
+    pos = [t[k] for k in ("x", "y", "z")]
+    vel = [t[k] for k in ("vx", "vy", "vz")]
+    acc = [torch.full((n,), 1e-3, dtype=torch.float64, device="cuda") for _ in range(3)]
+    vh = [torch.zeros_like(a) for a in acc]
+    out = torch.zeros(4, dtype=torch.float64, device="cuda")
+    ke = min(n, n_energy)
+    for _ in range(3):
+        ctx.kick_drift(vh, vel, pos, acc, DT)
+        ctx.kick(vel, vh, acc, DT)
+    for _ in range(3):
+        ctx.energy(t["m"][:ke], *[a[:ke] for a in pos], *[v[:ke] for v in vel], d["G"], out)
+    ctx.sync()
+
+
 CASES = {
     "pair": lambda a: pair_case(int(a[0]) if a else 262144, int(a[1]) if len(a) > 1 else 0),
     "sym": lambda a: pair_case(int(a[0]) if a else 262144, int(a[1]) if len(a) > 1 else 0, True),
@@ -789,6 +814,7 @@ CASES = {
     "df64": lambda a: df64_case(int(a[0]) if a else 262144),
     "batch": lambda a: batch_case(int(a[0]) if a else 512, int(a[1]) if len(a) > 1 else -1),
     "build": lambda a: build_case(int(a[0]) if a else 1 << 20, a[1] if len(a) > 1 else "fp64"),
+    "leapfrog": lambda a: leapfrog_case(int(a[0]) if a else 1 << 20),
 }
 
 

@@ -113,6 +113,29 @@ def test_range_matches_full(ctx):
         assert np.all(part[:1000] == 0) and np.all(part[2100:] == 0)
 
 
+@pytest.mark.parametrize("ws", [2, 3])
+def test_target_shards_gather_to_the_full_result(ctx, ws):
+    """The replica logic's target split (nbody.replicas.target_range) on the GPU hook: every
+    rank's shard computed by nb_naive_accel_range and gathered equals the single call bit for bit
+    (NB_F64_IEEE), as the ranks of a sharded run would produce it."""
+    import torch
+    from nbody.replicas import target_range
+    n = 2501
+    d = bodies("plummer", n, seed=4)
+    t = {k: dev(d[k]) for k in ("m", "x", "y", "z")}
+    full = run_naive(ctx, d, 1e-6, "f64_ieee")
+    gathered = [np.zeros(n) for _ in range(3)]
+    for rank in range(ws):
+        b, e = target_range(n, rank, ws)
+        acc = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+        ctx.naive_accel_range(t["m"], t["x"], t["y"], t["z"], *acc, b, e, 1.0, 1e-6, "f64_ieee")
+        ctx.sync()
+        for g, a in zip(gathered, acc):
+            g[b:e] = host(a)[b:e]
+    for g, f in zip(gathered, full):
+        np.testing.assert_array_equal(g, f)
+
+
 def test_invalid_arguments_are_reported(ctx):
     import torch
     from nbody.lib import NBodyError
