@@ -6,11 +6,20 @@
 // "Accept" (or skip) continues at the skip link and "open" continues at the next node, so a
 // traversal needs no stack at all and visits nodes in exactly the reference's order.
 //
-//  * per-body rule (NB_OPEN_THETA): the 32 lanes of a warp hold 32 bodies adjacent in tree order,
-//    each with its own position in the DFS sequence. Every iteration the warp takes the smallest
-//    position (__reduce_min_sync) and the lanes sitting on it evaluate that node -- one broadcast
-//    load -- and advance by their own decision. Each body sees the reference's sequence of
-//    accepted nodes in the reference's order.
+//  * per-body rule (NB_OPEN_THETA), default schedule (bh_theta_lane_kernel, FP64; and
+//    bh_theta_df_kernel, double-float): each lane walks its own body's DFS sequence, deciding each
+//    cell with an FP32 pre-test whose rounding margin is proven and the reference's FP64
+//    expression only inside that margin; find-then-compute, so the FP64 monopoles of all lanes
+//    that found one run together. Warps take groups of 32 bodies close together in the tree, after
+//    the first traversal of a tree sorted within windows of 1,024 by the length of their last
+//    walk, so that the lanes of a warp finish together.
+//  * per-body rule, lockstep schedule (bh_theta_f64_kernel, nb_bh_set_schedule(1)): the 32 lanes
+//    of a warp hold 32 bodies adjacent in tree order, each with its own position in the DFS
+//    sequence. Every iteration the warp takes the smallest position (__reduce_min_sync) and the
+//    lanes sitting on it evaluate that node -- one broadcast load -- and advance by their own
+//    decision.
+//    Either way each body sees the reference's sequence of accepted nodes in the reference's
+//    order.
 //  * group rule (NB_OPEN_THETA_GROUP): the warp walks one sequence; a cell is opened when any
 //    lane's rule opens it, otherwise all lanes accept it -- no divergence.
 #include <algorithm>
