@@ -15,10 +15,10 @@
 //     leftmost split of each cell ("first split") stands for the cell.
 //  6. DFS numbering: each sorted position p starts popc(mask[p]) internal cells plus its leaf;
 //     an exclusive scan gives every node its DFS pre-order index and skip link.
-//  7. bottom-up centre of mass: leaves one thread each, cells by blocks over chunks of sorted
-//     positions (deepest level first), cells reaching past their chunk by the last child to
-//     arrive; children summed in octant order 0..7 (bit-identical to
-//     BarnesHutOctree.cpp:304-311), node records written with the sums.
+//  7. bottom-up centre of mass: leaves one thread each, cells by blocks over chunks of 4,096
+//     sorted positions (deepest level first), the cells reaching past their chunk (at most one
+//     per level) by tiers of blocks over 64 chunks each; children summed in octant order 0..7
+//     (bit-identical to BarnesHutOctree.cpp:304-311), node records written with the sums.
 #include <algorithm>
 
 #include "nb_bh.cuh"

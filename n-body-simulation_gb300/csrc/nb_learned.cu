@@ -11,11 +11,14 @@
 //    cell's monopole.
 //  * Training (nb_mlp_loss_grad, nb_mlp_adam): FP32 forward/backward kernels, MSE loss, Adam.
 //  * Inference (nb_bh_accel with NB_OPEN_LEARNED): each warp keeps a stack of cells in shared
-//    memory, pops up to 16 at a time and scores them with BF16 tensor-core mma.sync.m16n8k16
-//    (FP32 accumulate); each layer's accumulator fragments are reused in registers as the next
-//    layer's A fragments. Body leaves are always accepted, cells that may overlap the group are
-//    always opened, and cells with more bodies than the training range fall back to the group
-//    theta rule.
+//    memory, pops up to 32 at a time and scores the network's cells with BF16 tensor-core
+//    mma.sync.m16n8k16 (FP32 accumulate, one or two 16-row blocks); each layer's accumulator
+//    fragments are reused in registers as the next layer's A fragments. Body leaves are always
+//    accepted, cells that may overlap the group are always opened, cells whose analytic monopole
+//    error bound is below tau are accepted without the network, and cells with more bodies than
+//    the training range fall back to the group theta rule. Accepted monopoles and the bodies of
+//    small opened cells go to a per-warp interaction list summed by all lanes. Groups whose walk
+//    cost at least twice the mean in the previous launch are walked first.
 #include <cuda_bf16.h>
 
 #include "nb_bh.cuh"
